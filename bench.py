@@ -1,0 +1,505 @@
+#!/usr/bin/env python
+"""Benchmark of the streamParanumal streaming suite on GB300.
+
+One step = one pass of the FP64 BS1-BS8 suite, each kernel called exactly as the
+reference's drivers call it:
+  BS1 copy, BS2 axpy, BS3 norm (bs3_1+bs3_2), BS4 dot (bs4_1+bs4_2), BS5 CG update
+  (bs5_1+bs5_2) on vectors of N = 2^28 doubles (the top of the 2^10..2^28 sweep), and
+  BS6 gather, BS7 scatter, BS8 gather+scatter on a 64x64x64 hex box at p=7 whose
+  element slots are permuted from a seed (134,217,728 local / 90,518,849 global nodes).
+value = sum of the reference's accounted bytes (bs{1..8}Run.cpp) / step time, GB/s.
+Inputs are seeded synthetic data (no dataset is involved); every vector is larger
+than the 129 MB L2, so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the same path (oracle/, OpenMP on all
+host cores) on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BS1-8 HBM GB/s (reference byte accounting), FP64 suite"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nlog2", type=int, default=28, help="vector length 2^k for BS1-BS5")
+    ap.add_argument("--mesh", type=int, default=64, help="box edge in elements for BS6-BS8")
+    ap.add_argument("--p", type=int, default=7)
+    ap.add_argument("--perm-seed", type=int, default=20240607)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-nlog2", type=int, default=24)
+    ap.add_argument("--cpu-mesh", type=int, default=32)
+    ap.add_argument("--json-out", default=None)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- byte accounting
+def bytes_bs(N: int) -> dict:
+    """bs1Run.cpp:82-84, bs2Run.cpp:85-87, bs3Run.cpp:90-92, bs4Run.cpp:90-92,
+    bs5Run.cpp:94-96."""
+    return {"BS1": 16 * N, "BS2": 24 * N, "BS3": 8 * N, "BS4": 16 * N, "BS5": 24 * N}
+
+
+def bytes_ogs(Nt: int, Ng: int, val: int = 8) -> dict:
+    """bs6Run.cpp:58-63, bs7Run.cpp:58-63, bs8Run.cpp:56-61 (dlong = 4 bytes)."""
+    return {"BS6": (Ng + 1) * 4 + Nt * 4 + Nt * val + Ng * val,
+            "BS7": (Ng + 1) * 4 + Nt * 4 + Ng * val + Nt * val,
+            "BS8": (Ng + 1) * 4 + Nt * 4 + 2 * Nt * val}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_gpu{gpu}_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+            self.t0 = time.time()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[4:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for _, _, r in rows:
+            for name, val in zip(names, r[1:]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": rows[0][1],
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic() -> dict:
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_sample(nlog2: int, mesh: int, p: int, perm_seed: int, seed: int, reps: int = 3):
+    """Times the oracle (OpenMP, all host cores) on a bounded sample of the
+    workload.  Returns (GB/s, description, cores)."""
+    import numpy as np
+
+    from oracle import oracle as orc
+
+    N = 1 << nlog2
+    a = orc.uniform(N, seed)
+    b = orc.uniform(N, seed + 1)
+    ids = orc.box_hex_ids(mesh, mesh, mesh, p, perm_seed)
+    csr = orc.ogs_setup(ids, kind=1, unique=True)
+    rs, ci = csr["rsT"], csr["ciT"]
+    Nt, Ng = ids.size, rs.size - 1
+    q = orc.uniform(Nt, seed + 2)
+    gq = np.zeros(Ng)
+    alpha, beta = 0.5, -0.25
+    nb256 = max(1, min((N + 255) // 256, 256))
+    nb1024 = max(1, min((N + 1023) // 1024, 1024))
+    lib = orc.load()
+    D = orc._d
+
+    def one_pass():
+        lib.or_bs1(N, D(a), D(b))
+        lib.or_bs2(N, alpha, D(a), beta, D(b), 1)
+        part = np.zeros(1024)
+        out = np.zeros(1)
+        lib.or_bs3_1(256, nb256, N, D(a), D(part), 1)
+        lib.or_finish(256, nb256, D(part), D(out))
+        lib.or_bs4_1(256, nb256, N, D(a), D(b), D(part), 1)
+        lib.or_finish(256, nb256, D(part), D(out))
+        lib.or_bs5_1(1024, nb1024, N, D(a), alpha, D(b), D(part), 1)
+        lib.or_finish(1024, nb1024, D(part), D(out))
+        lib.or_ogs_gather(1, 0, Ng, orc._i32(rs), orc._i32(ci), 1, gq.ctypes.data, q.ctypes.data)
+        lib.or_ogs_scatter(1, Ng, orc._i32(rs), orc._i32(ci), 1, q.ctypes.data, gq.ctypes.data)
+        lib.or_ogs_gather_scatter(1, 0, Ng, orc._i32(rs), orc._i32(ci), orc._i32(rs),
+                                  orc._i32(ci), 1, q.ctypes.data)
+
+    nbytes = sum(bytes_bs(N).values()) + sum(bytes_ogs(Nt, Ng).values())
+    one_pass()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        one_pass()
+        times.append(time.perf_counter() - t0)
+    gbs = nbytes / 1e9 / statistics.median(times)
+    desc = (f"oracle restatement (OpenMP) of the same FP64 suite at N=2^{nlog2} and a "
+            f"{mesh}^3 p={p} permuted box ({Nt} local nodes); median of {reps} passes")
+    return gbs, desc, os.cpu_count(), nbytes, statistics.median(times)
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    from streamparanumal_gb300 import _build
+
+    _build.build_oracle()
+    import numpy as np
+
+    from oracle import oracle as orc
+
+    N = 1 << args.cpu_nlog2
+    seed = args.seed
+    a = orc.uniform(N, seed)
+    b = orc.uniform(N, seed + 1)
+    mesh, p = args.cpu_mesh, args.p
+    ids = orc.box_hex_ids(mesh, mesh, mesh, p, args.perm_seed)
+    csr = orc.ogs_setup(ids, kind=1, unique=True)
+    rs, ci = csr["rsT"], csr["ciT"]
+    Nt, Ng = ids.size, rs.size - 1
+    q = orc.uniform(Nt, seed + 2)
+    gq = np.zeros(Ng)
+    lib = orc.load()
+    D = orc._d
+    nb256 = max(1, min((N + 255) // 256, 256))
+    nb1024 = max(1, min((N + 1023) // 1024, 1024))
+    part = np.zeros(1024)
+    out = np.zeros(1)
+
+    def step():
+        lib.or_bs1(N, D(a), D(b))
+        lib.or_bs2(N, 0.5, D(a), -0.25, D(b), 1)
+        lib.or_bs3_1(256, nb256, N, D(a), D(part), 1)
+        lib.or_finish(256, nb256, D(part), D(out))
+        lib.or_bs4_1(256, nb256, N, D(a), D(b), D(part), 1)
+        lib.or_finish(256, nb256, D(part), D(out))
+        lib.or_bs5_1(1024, nb1024, N, D(a), 0.5, D(b), D(part), 1)
+        lib.or_finish(1024, nb1024, D(part), D(out))
+        lib.or_ogs_gather(1, 0, Ng, orc._i32(rs), orc._i32(ci), 1, gq.ctypes.data, q.ctypes.data)
+        lib.or_ogs_scatter(1, Ng, orc._i32(rs), orc._i32(ci), 1, q.ctypes.data, gq.ctypes.data)
+        lib.or_ogs_gather_scatter(1, 0, Ng, orc._i32(rs), orc._i32(ci), orc._i32(rs),
+                                  orc._i32(ci), 1, q.ctypes.data)
+
+    nbytes = sum(bytes_bs(N).values()) + sum(bytes_ogs(Nt, Ng).values())
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    gbs = nbytes * args.steps / 1e9 / el
+    desc = (f"each step: the FP64 suite at N=2^{args.cpu_nlog2} and a {mesh}^3 p={p} "
+            f"permuted box ({Nt} local nodes), a bounded sample of the GPU workload")
+    line = {"metric": METRIC, "value": round(gbs, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded uniform[-1,1])", "impl": "reference",
+            "config": {"workload": "BS1-BS8 FP64 suite (CPU sample)", "n": N,
+                       "mesh": f"{mesh}^3 p={p} permuted", "bytes_per_step": nbytes},
+            "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": os.cpu_count(),
+                             "kind": "port", "sample": desc},
+            "e2e": {"value": round(gbs, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+
+    from oracle import oracle as orc  # input generation only (seeded uniform values)
+    from streamparanumal_gb300 import _build, capi, kernels
+    from streamparanumal_gb300 import ogs as O
+
+    _build.build_library()
+    capi.load()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    N = 1 << args.nlog2
+    mesh, p = args.mesh, args.p
+    # ---- inputs (host, pinned) and plans
+    t_setup = time.time()
+    h_a = torch.from_numpy(orc.uniform(N, args.seed)).pin_memory()
+    h_b = torch.from_numpy(orc.uniform(N, args.seed + 1)).pin_memory()
+    ids = O.box_hex_ids(mesh, mesh, mesh, p, args.perm_seed)
+    Nt = ids.size
+    h_q = torch.from_numpy(orc.uniform(Nt, args.seed + 2)).pin_memory()
+    h = O.ogs_t()
+    with torch.cuda.stream(stream):
+        h.Setup(Nt, ids, kind=O.Signed, unique=True, stream=stream)
+    Ng = h.NgatherGlobal
+    del ids
+    a = h_a.to(dev)
+    b = h_b.to(dev)
+    q = h_q.to(dev)
+    gq = torch.zeros(Ng, dtype=torch.float64, device=dev)
+    tmp = torch.zeros(1024, dtype=torch.float64, device=dev)
+    scal = torch.zeros(4, dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(args.seed)
+    alpha, beta = (float(x) for x in rng.uniform(-1, 1, size=2))
+    nb256 = kernels.nblocks_for(N, 256)
+    nb1024 = kernels.nblocks_for(N, 1024)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t_setup
+
+    names = ["BS1", "BS2", "BS3", "BS4", "BS5", "BS6", "BS7", "BS8"]
+    nbytes = {**bytes_bs(N), **bytes_ogs(Nt, Ng)}
+    step_bytes = sum(nbytes.values())
+    call = capi.call
+
+    def suite():
+        call("sp_bs1_copy_f64", N, a.data_ptr(), b.data_ptr(), sptr)
+        yield "BS1"
+        call("sp_bs2_axpy_f64", N, alpha, a.data_ptr(), beta, b.data_ptr(), sptr)
+        yield "BS2"
+        call("sp_bs3_1_f64", 256, nb256, N, a.data_ptr(), tmp.data_ptr(), sptr)
+        call("sp_reduce_finish_f64", 256, nb256, tmp.data_ptr(), scal.data_ptr(), sptr)
+        yield "BS3"
+        call("sp_bs4_1_f64", 256, nb256, N, a.data_ptr(), b.data_ptr(), tmp.data_ptr(), sptr)
+        call("sp_reduce_finish_f64", 256, nb256, tmp.data_ptr(), scal.data_ptr() + 8, sptr)
+        yield "BS4"
+        call("sp_bs5_1_f64", 1024, nb1024, N, a.data_ptr(), alpha, b.data_ptr(), tmp.data_ptr(),
+             sptr)
+        call("sp_reduce_finish_f64", 1024, nb1024, tmp.data_ptr(), scal.data_ptr() + 16, sptr)
+        yield "BS5"
+        h.Gather(gq, q, 1, O.Add, O.Trans, stream=stream)
+        yield "BS6"
+        h.Scatter(q, gq, 1, O.NoTrans, stream=stream)
+        yield "BS7"
+        h.GatherScatter(q, 1, O.Add, O.Sym, stream=stream)
+        yield "BS8"
+
+    def run_steps(k, events=None):
+        for s in range(k):
+            if events is not None:
+                events[s][0].record(stream)
+            for i, _ in enumerate(suite()):
+                if events is not None:
+                    events[s][i + 1].record(stream)
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+    # ---- warm-up
+    run_steps(args.warmup)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    # ---- timed region (device events on the launching stream)
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+              for _ in range(args.steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    capi.load().sp_launch_count_reset()
+    start.record(stream)
+    run_steps(args.steps, events)
+    end.record(stream)
+    torch.cuda.synchronize()
+    launches = int(capi.load().sp_launch_count())
+    if dist:
+        tdist.barrier()
+    total_ms = start.elapsed_time(end)
+    # keep the clock sampler running over a short soak of the same work so the
+    # record covers at least ~1 s under load
+    t_soak = time.time()
+    while time.time() - t_soak < 1.0:
+        run_steps(5)
+        torch.cuda.synchronize()
+    clocks = sampler.stop()
+    per = {n: 0.0 for n in names}
+    for ev in events:
+        for i, n in enumerate(names):
+            per[n] += ev[i].elapsed_time(ev[i + 1])
+    per = {n: v / args.steps for n, v in per.items()}  # ms per call
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * step_bytes / 1e9 / (ms_per_step / 1e3)
+
+    # ---- e2e: host buffers, H2D of the step's inputs and D2H of its results timed
+    h_out_b = torch.empty_like(h_b).pin_memory()
+    h_out_q = torch.empty_like(h_q).pin_memory()
+    h_scal = torch.empty(4, dtype=torch.float64).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            a.copy_(h_a, non_blocking=True)
+            b.copy_(h_b, non_blocking=True)
+            q.copy_(h_q, non_blocking=True)
+            for _ in suite():
+                pass
+            h_out_b.copy_(b, non_blocking=True)
+            h_out_q.copy_(q, non_blocking=True)
+            h_scal.copy_(scal, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        tdist.barrier()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = (h_a.numel() + h_b.numel() + h_q.numel()) * 8
+    d2h = (h_out_b.numel() + h_out_q.numel() + h_scal.numel()) * 8
+    e2e_value = world * step_bytes / 1e9 / (e2e_ms / 1e3)
+
+    # ---- BS0 launch latency: 10,000 empty launches, plain and graph-captured
+    bs0 = bs0_latency(stream, dev)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    dom = max(names, key=lambda n: per[n])
+    achieved = nbytes[dom] / 1e9 / (per[dom] / 1e3)
+    traffic = ncu_traffic().get(dom)
+    detail = {n: {"ms": round(per[n], 4), "bytes": nbytes[n],
+                  "GBps": round(nbytes[n] / 1e9 / (per[n] / 1e3), 1),
+                  "frac_of_peak": round(nbytes[n] / 1e9 / (per[n] / 1e3) / peak, 4)}
+              for n in names}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform[-1,1] FP64; seeded element permutation)",
+        "config": {"workload": f"BS1-BS8 FP64 suite: BS1-BS5 at N=2^{args.nlog2}, BS6/BS7/BS8 "
+                               f"on a {mesh}^3 hex box at p={p}, permuted elements",
+                   "n": N, "local_nodes": Nt, "global_nodes": Ng, "bytes_per_step": step_bytes,
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind, "traffic": traffic},
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "detail": {"per_kernel": detail, "bs0_us_per_launch": bs0,
+                   "setup_s": round(t_setup, 2)},
+    }
+    if not args.no_cpu_baseline:
+        gbs, desc, cores, _, _ = cpu_sample(args.cpu_nlog2, args.cpu_mesh, p, args.perm_seed,
+                                            args.seed)
+        line["cpu_baseline"] = {"value": round(gbs, 3), "unit": UNIT, "cores": cores,
+                                "kind": "port", "sample": desc}
+    print(json.dumps(line), flush=True)
+    if args.json_out:
+        Path(args.json_out).write_text(json.dumps(line, indent=1))
+
+
+def bs0_latency(stream, dev) -> dict:
+    """bs0Run.cpp:68-79: host time of n back-to-back empty launches plus one
+    synchronisation, divided by n; and the same n launches replayed from one graph."""
+    import torch
+
+    from streamparanumal_gb300 import capi
+
+    a = torch.zeros(1, dtype=torch.float64, device=dev)
+    b = torch.zeros(1, dtype=torch.float64, device=dev)
+    lib = capi.load()
+    sptr = stream.cuda_stream
+    n = 10000
+    for _ in range(100):
+        lib.sp_bs0(1, a.data_ptr(), b.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        lib.sp_bs0(1, a.data_ptr(), b.data_ptr(), sptr)
+    stream.synchronize()
+    plain = (time.perf_counter() - t0) / n * 1e6
+    g = capi.ctypes.c_void_p()
+    capi.call("sp_bs0_graph_create", n, 1, a.data_ptr(), b.data_ptr(), sptr, capi.ctypes.byref(g))
+    lib.sp_graph_launch(g, sptr)
+    stream.synchronize()
+    t0 = time.perf_counter()
+    lib.sp_graph_launch(g, sptr)
+    stream.synchronize()
+    graph = (time.perf_counter() - t0) / n * 1e6
+    lib.sp_graph_destroy(g)
+    return {"plain": round(plain, 3), "graph": round(graph, 3), "launches": n}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+/*
+ * sp_capi.h -- C ABI of the GB300 (sm_103a) streaming hot path of streamParanumal.
+ *
+ * This is the boundary that replaces the OCCA device behind the reference's
+ * platform_t / kernel_t / deviceMemory<T> / ogs::ogs_t objects.  Every entry point
+ * takes plain pointers and sizes, runs on an explicit CUDA stream, and returns an
+ * sp_status instead of throwing (the reference aborts through LIBP_ABORT,
+ * include/utils.hpp:69; the C++ mirror in streamparanumal_gb300/host turns a
+ * non-success status back into that exception).
+ *
+ * Conventions
+ *  - Device pointers are plain CUDA device addresses.  Host pointers are named
+ *    h_* and are only read during the call.
+ *  - All launches are asynchronous on `stream` (NULL = legacy default stream).
+ *    No entry point synchronises the device except the *_create/setup calls,
+ *    which copy plan data to the device.
+ *  - Vector lengths are int64_t; ogs indices are int32_t (the reference's dlong,
+ *    include/types.h:60) and ogs ids are int64_t (hlong, include/types.h:52).
+ *  - After a failing call, sp_last_error_string() describes the failure
+ *    (per host thread).
+ */
+#ifndef SP_CAPI_H
+#define SP_CAPI_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* sp_stream_t; /* identical to cudaStream_t */
+
+typedef int32_t sp_status;
+#define SP_SUCCESS            0
+#define SP_ERR_INVALID_ARG    1  /* null pointer, negative size, bad enum          */
+#define SP_ERR_CUDA           2  /* a CUDA runtime call or launch failed            */
+#define SP_ERR_ALLOC          3  /* cudaMalloc / host allocation failed             */
+#define SP_ERR_UNSUPPORTED    4  /* a type/op/transpose combination not provided    */
+#define SP_ERR_SIZE           5  /* size exceeds an int32 index or a plan limit     */
+#define SP_ERR_CSR            6  /* malformed CSR / ids handed to a plan builder    */
+#define SP_ERR_TIMEOUT        7  /* a bounded device-side wait gave up              */
+#define SP_ERR_DEVICE_CHECK   8  /* a device-side bounds check recorded a bad index */
+
+/* ogs enums: same values as the reference's ogs::Type / Op / Transpose / Kind
+ * (include/ogs.hpp:179-200). */
+typedef enum { SP_FLOAT = 0, SP_DOUBLE = 1, SP_INT32 = 2, SP_INT64 = 3 } sp_type;
+typedef enum { SP_OP_ADD = 0, SP_OP_MUL = 1, SP_OP_MAX = 2, SP_OP_MIN = 3 } sp_op;
+typedef enum { SP_SYM = 0, SP_NOTRANS = 1, SP_TRANS = 2 } sp_transpose;
+typedef enum { SP_KIND_UNSIGNED = 0, SP_KIND_SIGNED = 1, SP_KIND_HALO = 2 } sp_kind;
+
+/* ---------------------------------------------------------------- library */
+const char* sp_last_error_string(void);
+const char* sp_status_string(sp_status s);
+int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch */
+/* Number of kernel launches issued by this library on the calling host thread
+ * since the last reset (used by harnesses to count launches in a timed region). */
+int64_t     sp_launch_count(void);
+void        sp_launch_count_reset(void);
+
+/* ---------------------------------------------------------------- BS0
+ * Empty 1x1 launch.  Replaces the `bs0` kernel (BS/BS0/okl/bs0.okl:27-39) launched
+ * by bs0_t::Run (BS/BS0/src/bs0Run.cpp:72). Writes b[0]=0 only if n==0. */
+sp_status sp_bs0(int32_t n, const double* a, double* b, sp_stream_t stream);
+
+/* BS0 graph form: capture `nlaunches` empty kernels into one CUDA graph once,
+ * then replay it with a single launch (collapses the per-launch host cost). */
+typedef struct sp_graph sp_graph;
+sp_status sp_bs0_graph_create(int32_t nlaunches, int32_t n, const double* a, double* b,
+                              sp_stream_t stream, sp_graph** out);
+sp_status sp_graph_launch(const sp_graph* g, sp_stream_t stream);
+sp_status sp_graph_destroy(sp_graph* g);
+
+/* ---------------------------------------------------------------- BS1 copy
+ * b[n] = a[n].  Replaces `bs1` (BS/BS1/okl/bs1.okl:27-34), called at
+ * BS/BS1/src/bs1Run.cpp:76 as kernel(N, o_a, o_b).  Bit-exact. */
+sp_status sp_bs1_copy_f64(int64_t n, const double* a, double* b, sp_stream_t stream);
+sp_status sp_bs1_copy_f32(int64_t n, const float* a, float* b, sp_stream_t stream);
+
+/* ---------------------------------------------------------------- BS2 axpy
+ * y[n] = alpha*x[n] + beta*y[n].  Replaces `bs2` (BS/BS2/okl/bs2.okl:27-36),
+ * called at BS/BS2/src/bs2Run.cpp:79 as kernel(N, alpha, o_x, beta, o_y).
+ * FP64 rounding follows the reference's CUDA mode (--fmad=true,
+ * libs/core/platformProperties.cpp:76): y = fma(alpha, x, beta*y). */
+sp_status sp_bs2_axpy_f64(int64_t n, double alpha, const double* x, double beta, double* y,
+                          sp_stream_t stream);
+sp_status sp_bs2_axpy_f32(int64_t n, float alpha, const float* x, float beta, float* y,
+                          sp_stream_t stream);
+
+/* ---------------------------------------------------------------- BS3/BS4/BS5
+ * Order-exact two-stage reductions: the same partition and summation tree as the
+ * reference's kernels, so results are bit-identical to its CUDA mode.
+ *   stage 1: nblocks logical blocks of `block_size` (256 or 1024) lanes; lane t of
+ *            block b accumulates ids t + b*bs + j*bs*nblocks in order, then a
+ *            halving tree writes partial[b].
+ *   stage 2: one block sums partial[0..nblocks) with the same tree into out[0].
+ * BS3  bs3_1/bs3_2 (BS/BS3/okl/bs3.okl:27-102; call sites bs3Run.cpp:83-84):
+ *        partial = sum a*a                      (no sqrt)
+ * BS4  bs4_1/bs4_2 (BS/BS4/okl/bs4.okl:27-103; bs4Run.cpp:83-84):  sum a*b
+ * BS5  bs5_1/bs5_2 (BS/BS5/okl/bs5.okl:27-106; bs5Run.cpp:87-88):
+ *        r = r + alpha*Ap (stored), partial = sum r*r
+ * nblocks must be in [1, block_size]; block_size in {256, 512, 1024}. */
+sp_status sp_bs3_1_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* a,
+                       double* partial, sp_stream_t stream);
+sp_status sp_bs4_1_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* a,
+                       const double* b, double* partial, sp_stream_t stream);
+sp_status sp_bs5_1_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* Ap,
+                       double alpha, double* r, double* partial, sp_stream_t stream);
+/* Stage 2, shared by bs3_2 / bs4_2 / bs5_2 (identical kernels in the reference). */
+sp_status sp_reduce_finish_f64(int32_t block_size, int32_t nblocks, const double* partial,
+                               double* out, sp_stream_t stream);
+
+/* ---------------------------------------------------------------- fast reductions
+ * Single-launch reductions over a fixed grid (deterministic for a given n, but
+ * not the reference's summation order).  `scratch` must hold
+ * sp_reduce_scratch_bytes() bytes and be zero-filled before its first use; every
+ * call leaves it zero-filled again.  Calls sharing one scratch must not overlap
+ * on the device.  Results go to the device scalar out[0] (FP64).
+ * FP32-storage forms accumulate in FP32 with compensated (TwoSum) per-lane
+ * partials and finalise across blocks in FP64. */
+size_t    sp_reduce_scratch_bytes(void);
+sp_status sp_norm2_f64(int64_t n, const double* a, double* out, void* scratch, sp_stream_t stream);
+sp_status sp_dot_f64(int64_t n, const double* a, const double* b, double* out, void* scratch,
+                     sp_stream_t stream);
+sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch, sp_stream_t stream);
+sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, void* scratch,
+                     sp_stream_t stream);
+
+/* ---------------------------------------------------------------- CG update
+ * Full CG update (the spec form; the reference's BS5 only does the r update):
+ *   x += alpha*p;  r -= alpha*Ap;  rdotr[0] = sum r*r   (FP64 result)
+ * x = fma(alpha, p, x), r = fma(-alpha, Ap, r), accumulation fma(r, r, acc).
+ * Scratch rules as for the fast reductions. */
+sp_status sp_cg_update_f64(int64_t n, double alpha, const double* p, const double* Ap,
+                           double* x, double* r, double* rdotr, void* scratch,
+                           sp_stream_t stream);
+sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float* Ap,
+                           float* x, float* r, double* rdotr, void* scratch,
+                           sp_stream_t stream);
+
+/* ---------------------------------------------------------------- ogs
+ * A gather-scatter plan is the device form of the reference's local
+ * ogsOperator_t (include/ogs/ogsOperator.hpp:44-138): a T operator (all members
+ * of each group) and an N operator (positive members only) in CSR, plus a row
+ * partition into blocks of at most sp_ogs_block_nnz() non-zeros.
+ * Rows/columns follow ogsBase_t::Setup (libs/ogs/ogsSetup.cpp:87-290): rows are
+ * groups in order of first appearance (positive groups first), columns ascending
+ * local index inside each row.  Sums run in that column order from the op's
+ * identity, so FP64/FP32 results are bit-identical to the reference. */
+typedef struct sp_ogs_plan sp_ogs_plan;
+
+typedef struct {
+  int32_t N;          /* local vector length the plan acts on                  */
+  int32_t NrowsT;     /* rows of the T operator (= Ngather on one rank)         */
+  int32_t NrowsN;     /* rows with a positive member                           */
+  int32_t nnzT;       /* entries in the T operator                             */
+  int32_t nnzN;       /* entries in the N operator                             */
+  int32_t NrowBlocksT;
+  int32_t NrowBlocksN;
+  int32_t maxRowSize; /* largest group                                          */
+  int64_t NgatherGlobal;
+} sp_ogs_info;
+
+/* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):
+ * h_ids[N] (0 = ignored, negative = flagged).  With unique != 0 exactly one member
+ * of every group is made positive and the signs are written back into h_ids
+ * (as the reference does).  Host-side setup plus device upload on `stream`. */
+sp_status sp_ogs_setup(int32_t N, int64_t* h_ids, sp_kind kind, int32_t unique,
+                       sp_stream_t stream, sp_ogs_plan** out);
+/* Host half of sp_ogs_setup: fills the T and N CSR without touching the device.
+ * rowStarts* need N+1 entries and colIds* N entries. */
+sp_status sp_ogs_setup_csr(int32_t N, int64_t* h_ids, sp_kind kind, int32_t unique,
+                           int32_t* NrowsT, int32_t* h_rowStartsT, int32_t* h_colIdsT,
+                           int32_t* NrowsN, int32_t* h_rowStartsN, int32_t* h_colIdsN);
+/* Build from an explicit CSR (T operator) and optional N operator.  Passing NULL
+ * h_rowStartsN/h_colIdsN makes the N operator share T's CSR over T's first NrowsN
+ * rows (NrowsN < 0 or > NrowsT: all rows), as for an Unsigned handle. */
+sp_status sp_ogs_plan_create(int32_t N, int32_t NrowsT, const int32_t* h_rowStartsT,
+                             const int32_t* h_colIdsT, int32_t NrowsN,
+                             const int32_t* h_rowStartsN, const int32_t* h_colIdsN,
+                             sp_stream_t stream, sp_ogs_plan** out);
+sp_status sp_ogs_plan_destroy(sp_ogs_plan* plan);
+sp_status sp_ogs_plan_info(const sp_ogs_plan* plan, sp_ogs_info* info);
+/* Copy the host CSR of one operator (trans = SP_TRANS -> T, SP_NOTRANS -> N) into
+ * caller arrays sized NrowsX+1 and nnzX (either pointer may be NULL). */
+sp_status sp_ogs_plan_csr(const sp_ogs_plan* plan, sp_transpose which, int32_t* h_rowStarts,
+                          int32_t* h_colIds);
+int32_t   sp_ogs_block_nnz(void);
+
+/* ogs_t::Gather   (include/ogs.hpp:289-293; libs/ogs/ogs.cpp:205-301;
+ *                  kernel libs/ogs/okl/ogsKernels.okl:86-122)
+ *   gv[row*k + f] = op over members c of row (CSR order) of v[col(c)*k + f]
+ *   trans == SP_NOTRANS uses the N operator, otherwise T.
+ * ogs_t::Scatter  (include/ogs.hpp:327-330; ogs.cpp:394-492; ogsKernels.okl:127-164)
+ *   v[col(c)*k + f] = gv[row*k + f]; trans == SP_TRANS uses N, otherwise T.
+ * ogs_t::GatherScatter (include/ogs.hpp:251-254; ogs.cpp:39-125; ogsKernels.okl:32-81)
+ *   Sym: gather T / scatter T; NoTrans: gather N / scatter T; Trans: gather T /
+ *   scatter N.  The op is honoured for every transpose (the reference's device
+ *   path always uses Add, libs/ogs/ogsOperator.cpp:448). */
+sp_status sp_ogs_gather(const sp_ogs_plan* plan, sp_type type, sp_op op, sp_transpose trans,
+                        int32_t k, void* gv, const void* v, sp_stream_t stream);
+sp_status sp_ogs_scatter(const sp_ogs_plan* plan, sp_type type, sp_transpose trans, int32_t k,
+                         void* v, const void* gv, sp_stream_t stream);
+sp_status sp_ogs_gather_scatter(const sp_ogs_plan* plan, sp_type type, sp_op op,
+                                sp_transpose trans, int32_t k, void* v, sp_stream_t stream);
+
+/* ---------------------------------------------------------------- box mesh ids
+ * Global node ids of a structured nx*ny*nz hex box of degree p on one rank, as
+ * mesh_t::Setup produces them (SetupBoxHex3D libs/mesh/meshSetupBoxHex3D.cpp:87-130,
+ * ConnectNodes libs/mesh/meshConnectNodes.cpp:43-81): id(l) = 1 + the smallest local
+ * index l' = e'*Np + n' that sits on the same lattice point.  With perm_seed != 0 the
+ * element slots are first permuted by a seeded Fisher-Yates shuffle (SplitMix64
+ * stream), slot(e) = perm[e].  h_ids must hold nx*ny*nz*(p+1)^3 entries. */
+sp_status sp_mesh_box_hex_ids(int32_t nx, int32_t ny, int32_t nz, int32_t p, uint64_t perm_seed,
+                              int64_t* h_ids);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SP_CAPI_H */

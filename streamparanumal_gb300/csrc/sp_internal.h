@@ -1,0 +1,48 @@
+// Internal helpers shared by the CUDA translation units of libspgb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/sp_capi.h"
+
+namespace sp {
+
+// Records a formatted message as this host thread's last error and returns `s`.
+sp_status fail(sp_status s, const char* fmt, ...);
+// Clears the last error message.
+void clear_error();
+// Counts one kernel launch issued by the library on this host thread.
+void count_launch(int64_t n = 1);
+
+// Checks the launch that was just issued (configuration errors only: no sync).
+inline sp_status check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(SP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  count_launch();
+  return SP_SUCCESS;
+}
+
+inline cudaStream_t as_cuda(sp_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define SP_CUDA_TRY(expr)                                                              \
+  do {                                                                                 \
+    cudaError_t _e = (expr);                                                           \
+    if (_e != cudaSuccess)                                                             \
+      return ::sp::fail(SP_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(_e));  \
+  } while (0)
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// ---------------------------------------------------------------- scratch layout
+// Layout of the caller-provided scratch of the single-launch reductions:
+//   [0, 8)                 : unsigned int ticket counter (+4 bytes pad)
+//   [256, 256 + 16*kMaxRedBlocks) : per-block partials (two doubles per block)
+constexpr int    kMaxRedBlocks   = 2048;
+constexpr size_t kRedPartialOff  = 256;
+constexpr size_t kRedScratchSize = kRedPartialOff + 16 * (size_t)kMaxRedBlocks;
+
+}  // namespace sp

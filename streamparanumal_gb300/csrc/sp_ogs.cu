@@ -1,0 +1,555 @@
+// ogs gather / scatter / gather+scatter kernels and plan construction (sm_103a).
+//
+// Work decomposition: the rows of a CSR operator are cut into blocks of at most
+// kOgsBlockNnz non-zeros.  One CTA of 256 lanes owns one block:
+//   1. each lane loads up to 8 column ids of the block (coalesced) and issues the
+//      8 gathers of v ahead of use, staging the values in shared memory;
+//   2. one lane per row combines its values in CSR order, starting from the op's
+//      identity -- the same order as the reference (ogsKernels.okl:64-67,
+//      ogsOperator.cpp:382-385), hence bit-identical sums;
+//   3. the row results are written back coalesced (gather: by row; scatter and
+//      gather+scatter: by column slot, with the column ids still in registers).
+// Every column belongs to exactly one row, so in-place gather+scatter has no
+// cross-CTA hazard.
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "sp_ogs_plan.h"
+
+namespace sp {
+
+// ------------------------------------------------------------------ ops
+// Identities and update rules of libs/ogs/ogsUtils.cpp:62-103 (device) and
+// libs/ogs/ogsOperator.cpp:37-56 (host): Max/Min start from -+numeric max and
+// keep the current value unless the new one compares strictly greater/less.
+template <typename T> struct Lim;
+template <> struct Lim<float>  { static __device__ float big()  { return 3.402823466e+38f; } };
+template <> struct Lim<double> { static __device__ double big() { return 1.7976931348623157e+308; } };
+template <> struct Lim<int32_t> { static __device__ int32_t big() { return 2147483647; } };
+template <> struct Lim<long long> { static __device__ long long big() { return 9223372036854775807LL; } };
+
+template <typename T> __device__ __forceinline__ T wrap_add(T a, T b) { return a + b; }
+template <typename T> __device__ __forceinline__ T wrap_mul(T a, T b) { return a * b; }
+template <> __device__ __forceinline__ int32_t wrap_add(int32_t a, int32_t b) {
+  return (int32_t)((uint32_t)a + (uint32_t)b);
+}
+template <> __device__ __forceinline__ int32_t wrap_mul(int32_t a, int32_t b) {
+  return (int32_t)((uint32_t)a * (uint32_t)b);
+}
+template <> __device__ __forceinline__ long long wrap_add(long long a, long long b) {
+  return (long long)((unsigned long long)a + (unsigned long long)b);
+}
+template <> __device__ __forceinline__ long long wrap_mul(long long a, long long b) {
+  return (long long)((unsigned long long)a * (unsigned long long)b);
+}
+
+template <typename T, int OP> struct Op;
+template <typename T> struct Op<T, SP_OP_ADD> {
+  static __device__ __forceinline__ T init() { return T(0); }
+  static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_add(a, b); }
+};
+template <typename T> struct Op<T, SP_OP_MUL> {
+  static __device__ __forceinline__ T init() { return T(1); }
+  static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_mul(a, b); }
+};
+template <typename T> struct Op<T, SP_OP_MAX> {
+  static __device__ __forceinline__ T init() { return -Lim<T>::big(); }
+  static __device__ __forceinline__ void apply(T& a, T b) { a = (b > a) ? b : a; }
+};
+template <typename T> struct Op<T, SP_OP_MIN> {
+  static __device__ __forceinline__ T init() { return Lim<T>::big(); }
+  static __device__ __forceinline__ void apply(T& a, T b) { a = (b < a) ? b : a; }
+};
+
+// ------------------------------------------------------------------ kernels
+
+// Stage the block's gathered values: s[i] = v[k + col(g0+i)*K] for i < gn.
+// Lane-strided so that both the id loads and the shared stores are coalesced;
+// the column ids stay in registers for a later in-place scatter.
+template <typename T>
+__device__ __forceinline__ void stage_values(const int32_t* __restrict__ ids, int32_t g0,
+                                             int32_t gn, const T* __restrict__ v, int k, int K,
+                                             T* s, int32_t (&col)[kOgsPerLane]) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = tid + j * kOgsThreads;
+    col[j] = (i < gn) ? __ldg(ids + g0 + i) : 0;
+  }
+  T val[kOgsPerLane];
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = tid + j * kOgsThreads;
+    if (i < gn) val[j] = v[k + (int64_t)col[j] * K];
+  }
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = tid + j * kOgsThreads;
+    if (i < gn) s[i] = val[j];
+  }
+}
+
+// Gather+scatter with the same operator for both halves (ogs::Sym).
+template <typename T, int OP>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogs_gs_sym(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs,
+             const int32_t* __restrict__ ids, T* __restrict__ v, int K) {
+  __shared__ T s[kOgsBlockNnz];
+  const int k = blockIdx.y;
+  const int32_t r0 = __ldg(blocks + blockIdx.x), r1 = __ldg(blocks + blockIdx.x + 1);
+  const int32_t g0 = __ldg(rs + r0), gn = __ldg(rs + r1) - g0;
+  int32_t col[kOgsPerLane];
+  stage_values<T>(ids, g0, gn, v, k, K, s, col);
+  __syncthreads();
+  for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
+    const int32_t a = __ldg(rs + row) - g0, b = __ldg(rs + row + 1) - g0;
+    T acc = Op<T, OP>::init();
+    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
+    for (int32_t i = a; i < b; ++i) s[i] = acc;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = threadIdx.x + j * kOgsThreads;
+    if (i < gn) v[k + (int64_t)col[j] * K] = s[i];
+  }
+}
+
+// Gather+scatter with different gather (gS/gI) and scatter (sS/sI) operators
+// (ogs::NoTrans: N then T; ogs::Trans: T then N).  Blocks partition T rows.
+template <typename T, int OP>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogs_gs_gen(const int32_t* __restrict__ blocks, const int32_t* __restrict__ gS,
+             const int32_t* __restrict__ gI, const int32_t* __restrict__ sS,
+             const int32_t* __restrict__ sI, T* __restrict__ v, int K) {
+  __shared__ T s_in[kOgsBlockNnz];
+  __shared__ T s_out[kOgsBlockNnz];
+  const int k = blockIdx.y;
+  const int32_t r0 = __ldg(blocks + blockIdx.x), r1 = __ldg(blocks + blockIdx.x + 1);
+  const int32_t g0 = __ldg(gS + r0), gn = __ldg(gS + r1) - g0;
+  const int32_t s0 = __ldg(sS + r0), sn = __ldg(sS + r1) - s0;
+  int32_t col[kOgsPerLane];
+  stage_values<T>(gI, g0, gn, v, k, K, s_in, col);
+  __syncthreads();
+  for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
+    const int32_t a = __ldg(gS + row) - g0, b = __ldg(gS + row + 1) - g0;
+    T acc = Op<T, OP>::init();
+    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s_in[i]);
+    const int32_t c = __ldg(sS + row) - s0, d = __ldg(sS + row + 1) - s0;
+    for (int32_t i = c; i < d; ++i) s_out[i] = acc;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = threadIdx.x + j * kOgsThreads;
+    if (i < sn) v[k + (int64_t)__ldg(sI + s0 + i) * K] = s_out[i];
+  }
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogs_gather(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs,
+             const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv, int K) {
+  __shared__ T s[kOgsBlockNnz];
+  const int k = blockIdx.y;
+  const int32_t r0 = __ldg(blocks + blockIdx.x), r1 = __ldg(blocks + blockIdx.x + 1);
+  const int32_t g0 = __ldg(rs + r0), gn = __ldg(rs + r1) - g0;
+  int32_t col[kOgsPerLane];
+  stage_values<T>(ids, g0, gn, v, k, K, s, col);
+  __syncthreads();
+  for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
+    const int32_t a = __ldg(rs + row) - g0, b = __ldg(rs + row + 1) - g0;
+    T acc = Op<T, OP>::init();
+    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
+    gv[k + (int64_t)row * K] = acc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogs_scatter(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v, int K) {
+  __shared__ T s[kOgsBlockNnz];
+  const int k = blockIdx.y;
+  const int32_t r0 = __ldg(blocks + blockIdx.x), r1 = __ldg(blocks + blockIdx.x + 1);
+  const int32_t s0 = __ldg(rs + r0), sn = __ldg(rs + r1) - s0;
+  for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
+    const T x = gv[k + (int64_t)row * K];
+    const int32_t a = __ldg(rs + row) - s0, b = __ldg(rs + row + 1) - s0;
+    for (int32_t i = a; i < b; ++i) s[i] = x;
+  }
+  __syncthreads();
+  int32_t col[kOgsPerLane];
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = threadIdx.x + j * kOgsThreads;
+    col[j] = (i < sn) ? __ldg(ids + s0 + i) : 0;
+  }
+#pragma unroll
+  for (int j = 0; j < kOgsPerLane; ++j) {
+    const int i = threadIdx.x + j * kOgsThreads;
+    if (i < sn) v[k + (int64_t)col[j] * K] = s[i];
+  }
+}
+
+// ------------------------------------------------------------------ dispatch
+
+template <typename T, int OP>
+static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
+  if (p->NrowBlocksT == 0) return;
+  dim3 grid(p->NrowBlocksT, K);
+  if (trans == SP_SYM || p->n_is_t) {
+    k_ogs_gs_sym<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
+                                                     v, K);
+  } else if (trans == SP_NOTRANS) {  // gather N, scatter T
+    k_ogs_gs_gen<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsNpad,
+                                                     p->d_colIdsN, p->d_rowStartsT, p->d_colIdsT,
+                                                     v, K);
+  } else {  // SP_TRANS: gather T, scatter N
+    k_ogs_gs_gen<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
+                                                     p->d_rowStartsNpad, p->d_colIdsN, v, K);
+  }
+}
+
+template <typename T, int OP>
+static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
+                          cudaStream_t s) {
+  if (trans == SP_NOTRANS) {
+    if (p->NrowBlocksN == 0) return;
+    k_ogs_gather<T, OP><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
+        p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, v, gv, K);
+  } else {
+    if (p->NrowBlocksT == 0) return;
+    k_ogs_gather<T, OP><<<dim3(p->NrowBlocksT, K), kOgsThreads, 0, s>>>(
+        p->d_blocksT, p->d_rowStartsT, p->d_colIdsT, v, gv, K);
+  }
+}
+
+template <typename T>
+static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, const T* gv,
+                           cudaStream_t s) {
+  if (trans == SP_TRANS) {
+    if (p->NrowBlocksN == 0) return;
+    k_ogs_scatter<T><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
+        p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, gv, v, K);
+  } else {
+    if (p->NrowBlocksT == 0) return;
+    k_ogs_scatter<T><<<dim3(p->NrowBlocksT, K), kOgsThreads, 0, s>>>(
+        p->d_blocksT, p->d_rowStartsT, p->d_colIdsT, gv, v, K);
+  }
+}
+
+template <template <typename, int> class F, typename T, typename... A>
+static void by_op(sp_op op, A... a) {
+  switch (op) {
+    case SP_OP_ADD: F<T, SP_OP_ADD>::run(a...); break;
+    case SP_OP_MUL: F<T, SP_OP_MUL>::run(a...); break;
+    case SP_OP_MAX: F<T, SP_OP_MAX>::run(a...); break;
+    case SP_OP_MIN: F<T, SP_OP_MIN>::run(a...); break;
+  }
+}
+
+template <typename T, int OP> struct GsF {
+  static void run(const sp_ogs_plan* p, sp_transpose t, int K, void* v, cudaStream_t s) {
+    launch_gs<T, OP>(p, t, K, static_cast<T*>(v), s);
+  }
+};
+template <typename T, int OP> struct GatherF {
+  static void run(const sp_ogs_plan* p, sp_transpose t, int K, void* gv, const void* v,
+                  cudaStream_t s) {
+    launch_gather<T, OP>(p, t, K, static_cast<T*>(gv), static_cast<const T*>(v), s);
+  }
+};
+
+static sp_status check_common(const sp_ogs_plan* p, sp_type type, int32_t op, int32_t trans,
+                              int32_t k, const char* name) {
+  if (!p) return fail(SP_ERR_INVALID_ARG, "%s: null plan", name);
+  if (type < SP_FLOAT || type > SP_INT64) return fail(SP_ERR_INVALID_ARG, "%s: bad type", name);
+  if (op < SP_OP_ADD || op > SP_OP_MIN) return fail(SP_ERR_INVALID_ARG, "%s: bad op", name);
+  if (trans < SP_SYM || trans > SP_TRANS)
+    return fail(SP_ERR_INVALID_ARG, "%s: bad transpose", name);
+  if (k < 1 || k > 65535) return fail(SP_ERR_INVALID_ARG, "%s: k=%d outside [1,65535]", name, k);
+  return SP_SUCCESS;
+}
+
+// ------------------------------------------------------------------ plan construction
+
+bool partition_rows(int32_t nrows, const int32_t* rs, std::vector<int32_t>& blocks) {
+  blocks.clear();
+  blocks.push_back(0);
+  int32_t b0 = 0;
+  for (int32_t row = 0; row < nrows; ++row) {
+    if (rs[row + 1] - rs[row] > kOgsBlockNnz) return false;
+    if (rs[row + 1] - rs[b0] > kOgsBlockNnz || row - b0 >= kOgsBlockNnz) {
+      blocks.push_back(row);
+      b0 = row;
+    }
+  }
+  if (nrows > 0) blocks.push_back(nrows);
+  return true;
+}
+
+static sp_status validate_csr(int32_t N, int32_t nrows, const int32_t* rs, const int32_t* ids,
+                              const char* which, int32_t& maxRow) {
+  if (nrows < 0) return fail(SP_ERR_INVALID_ARG, "ogs plan: negative row count (%s)", which);
+  if (!rs) return fail(SP_ERR_INVALID_ARG, "ogs plan: null rowStarts (%s)", which);
+  if (rs[0] != 0) return fail(SP_ERR_CSR, "ogs plan: rowStarts[0] != 0 (%s)", which);
+  for (int32_t r = 0; r < nrows; ++r) {
+    const int32_t len = rs[r + 1] - rs[r];
+    if (len < 0) return fail(SP_ERR_CSR, "ogs plan: rowStarts not monotone at %d (%s)", r, which);
+    if (len > kOgsMaxRowSize)
+      return fail(SP_ERR_SIZE,
+                  "Multiplicity of a global node in ogsOperator_t::setupRowBlocks is too large "
+                  "(row %d has %d > %d members, %s)",
+                  r, len, kOgsMaxRowSize, which);
+    maxRow = std::max(maxRow, len);
+  }
+  const int32_t nnz = rs[nrows];
+  if (nnz > 0 && !ids) return fail(SP_ERR_INVALID_ARG, "ogs plan: null colIds (%s)", which);
+  for (int32_t i = 0; i < nnz; ++i)
+    if (ids[i] < 0 || ids[i] >= N)
+      return fail(SP_ERR_CSR, "ogs plan: colIds[%d]=%d outside [0,%d) (%s)", i, ids[i], N, which);
+  return SP_SUCCESS;
+}
+
+static void free_plan_device(sp_ogs_plan* p) {
+  if (p->own_n_csr) {
+    if (p->d_rowStartsNpad) cudaFree(p->d_rowStartsNpad);
+    if (p->d_colIdsN) cudaFree(p->d_colIdsN);
+  }
+  if (p->own_blocks_n && p->d_blocksN) cudaFree(p->d_blocksN);
+  int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
+  for (int32_t* q : ptrs)
+    if (q) cudaFree(q);
+  p->d_rowStartsT = p->d_colIdsT = p->d_blocksT = nullptr;
+  p->d_rowStartsNpad = p->d_colIdsN = p->d_blocksN = nullptr;
+  p->own_n_csr = p->own_blocks_n = false;
+}
+
+static sp_status upload(const std::vector<int32_t>& h, int32_t** d, cudaStream_t s) {
+  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(int32_t);
+  if (cudaMalloc(d, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *d = nullptr;
+    return fail(SP_ERR_ALLOC, "ogs plan: cudaMalloc of %zu bytes failed", bytes);
+  }
+  if (!h.empty()) SP_CUDA_TRY(cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(int32_t),
+                                              cudaMemcpyHostToDevice, s));
+  return SP_SUCCESS;
+}
+
+// Finishes a plan whose host CSR arrays are filled: validation, partition, upload.
+sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
+  int32_t maxRow = 0;
+  sp_status st = validate_csr(p->N, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), "T",
+                              maxRow);
+  if (st) return st;
+  p->nnzT = p->rowStartsT[p->NrowsT];
+  if (!p->n_is_t) {
+    if (p->NrowsN > p->NrowsT)
+      return fail(SP_ERR_CSR, "ogs plan: NrowsN %d > NrowsT %d", p->NrowsN, p->NrowsT);
+    st = validate_csr(p->N, p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), "N", maxRow);
+    if (st) return st;
+    p->nnzN = p->rowStartsN[p->NrowsN];
+    // every column at most once in T, and N's members of a row inside T's row
+    std::vector<int32_t> rowOf(std::max(p->N, 1), -1);
+    for (int32_t r = 0; r < p->NrowsT; ++r)
+      for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) {
+        if (rowOf[p->colIdsT[i]] != -1)
+          return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", p->colIdsT[i]);
+        rowOf[p->colIdsT[i]] = r;
+      }
+    for (int32_t r = 0; r < p->NrowsN; ++r)
+      for (int32_t i = p->rowStartsN[r]; i < p->rowStartsN[r + 1]; ++i)
+        if (rowOf[p->colIdsN[i]] != r)
+          return fail(SP_ERR_CSR, "ogs plan: N column %d of row %d is not in T row %d",
+                      p->colIdsN[i], r, r);
+  } else {
+    std::vector<uint8_t> seen(std::max(p->N, 1), 0);
+    for (int32_t i = 0; i < p->nnzT; ++i) {
+      if (seen[p->colIdsT[i]])
+        return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", p->colIdsT[i]);
+      seen[p->colIdsT[i]] = 1;
+    }
+    p->NrowsN = std::min(p->NrowsN, p->NrowsT);
+    p->rowStartsN.assign(p->rowStartsT.begin(), p->rowStartsT.begin() + p->NrowsN + 1);
+    p->colIdsN.assign(p->colIdsT.begin(), p->colIdsT.begin() + p->rowStartsN[p->NrowsN]);
+    p->nnzN = p->rowStartsN[p->NrowsN];
+  }
+  p->maxRowSize = maxRow;
+
+  // N partition: rows [0, NrowsN) of the N operator (which is T itself when
+  // n_is_t, e.g. for an Unsigned handle whose flagged-only groups follow).
+  std::vector<int32_t> blocksT, blocksN;
+  if (!partition_rows(p->NrowsT, p->rowStartsT.data(), blocksT) ||
+      !partition_rows(p->NrowsN, p->rowStartsN.data(), blocksN))
+    return fail(SP_ERR_SIZE, "ogs plan: a row exceeds the block capacity %d", kOgsBlockNnz);
+  p->NrowBlocksT = std::max<int32_t>(0, (int32_t)blocksT.size() - 1);
+  p->NrowBlocksN = std::max<int32_t>(0, (int32_t)blocksN.size() - 1);
+
+  SP_CUDA_TRY(cudaGetDevice(&p->device));
+  if ((st = upload(p->rowStartsT, &p->d_rowStartsT, s))) return st;
+  if ((st = upload(p->colIdsT, &p->d_colIdsT, s))) return st;
+  if ((st = upload(blocksT, &p->d_blocksT, s))) return st;
+  if (p->n_is_t) {
+    p->d_rowStartsNpad = p->d_rowStartsT;
+    p->d_colIdsN = p->d_colIdsT;
+  } else {
+    std::vector<int32_t> pad(p->rowStartsN);
+    pad.resize(p->NrowsT + 1, p->nnzN);  // rows without a positive member are empty
+    p->own_n_csr = true;
+    if ((st = upload(pad, &p->d_rowStartsNpad, s))) return st;
+    if ((st = upload(p->colIdsN, &p->d_colIdsN, s))) return st;
+  }
+  if (p->NrowsN == p->NrowsT && (p->n_is_t || blocksN == blocksT)) {
+    p->d_blocksN = p->d_blocksT;
+  } else {
+    p->own_blocks_n = true;
+    if ((st = upload(blocksN, &p->d_blocksN, s))) return st;
+  }
+  SP_CUDA_TRY(cudaStreamSynchronize(s));
+  return SP_SUCCESS;
+}
+
+}  // namespace sp
+
+using namespace sp;
+
+extern "C" {
+
+int32_t sp_ogs_block_nnz(void) { return kOgsBlockNnz; }
+
+sp_status sp_ogs_plan_create(int32_t N, int32_t NrowsT, const int32_t* h_rowStartsT,
+                             const int32_t* h_colIdsT, int32_t NrowsN, const int32_t* h_rowStartsN,
+                             const int32_t* h_colIdsN, sp_stream_t stream, sp_ogs_plan** out) {
+  if (!out) return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_create: null out");
+  *out = nullptr;
+  if (N < 0 || NrowsT < 0 || !h_rowStartsT)
+    return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_create: bad sizes or null rowStartsT");
+  sp_ogs_plan* p = new sp_ogs_plan();
+  p->N = N;
+  p->NrowsT = NrowsT;
+  p->rowStartsT.assign(h_rowStartsT, h_rowStartsT + NrowsT + 1);
+  const int32_t nnzT = h_rowStartsT[NrowsT];
+  if (nnzT < 0) {
+    delete p;
+    return fail(SP_ERR_CSR, "sp_ogs_plan_create: negative nnz");
+  }
+  if (nnzT > 0 && !h_colIdsT) {
+    delete p;
+    return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_create: null colIdsT");
+  }
+  p->colIdsT.assign(h_colIdsT, h_colIdsT + nnzT);
+  if (h_rowStartsN) {
+    if (NrowsN < 0) {
+      delete p;
+      return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_create: negative NrowsN");
+    }
+    p->n_is_t = false;
+    p->NrowsN = NrowsN;
+    p->rowStartsN.assign(h_rowStartsN, h_rowStartsN + NrowsN + 1);
+    const int32_t nnzN = h_rowStartsN[NrowsN];
+    if (nnzN < 0 || (nnzN > 0 && !h_colIdsN)) {
+      delete p;
+      return fail(SP_ERR_CSR, "sp_ogs_plan_create: bad N operator");
+    }
+    p->colIdsN.assign(h_colIdsN, h_colIdsN + nnzN);
+  } else {
+    p->n_is_t = true;
+    p->NrowsN = (NrowsN >= 0 && NrowsN <= NrowsT) ? NrowsN : NrowsT;
+  }
+  sp_status st = finalize_plan(p, as_cuda(stream));
+  if (st) {
+    free_plan_device(p);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return SP_SUCCESS;
+}
+
+sp_status sp_ogs_plan_destroy(sp_ogs_plan* p) {
+  if (!p) return SP_SUCCESS;
+  free_plan_device(p);
+  delete p;
+  return SP_SUCCESS;
+}
+
+sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
+  if (!p || !info) return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_info: null argument");
+  info->N = p->N;
+  info->NrowsT = p->NrowsT;
+  info->NrowsN = p->NrowsN;
+  info->nnzT = p->nnzT;
+  info->nnzN = p->nnzN;
+  info->NrowBlocksT = p->NrowBlocksT;
+  info->NrowBlocksN = p->NrowBlocksN;
+  info->maxRowSize = p->maxRowSize;
+  info->NgatherGlobal = p->NrowsN;
+  return SP_SUCCESS;
+}
+
+sp_status sp_ogs_plan_csr(const sp_ogs_plan* p, sp_transpose which, int32_t* rs, int32_t* ids) {
+  if (!p) return fail(SP_ERR_INVALID_ARG, "sp_ogs_plan_csr: null plan");
+  const std::vector<int32_t>& R = (which == SP_NOTRANS) ? p->rowStartsN : p->rowStartsT;
+  const std::vector<int32_t>& C = (which == SP_NOTRANS) ? p->colIdsN : p->colIdsT;
+  if (rs) std::memcpy(rs, R.data(), R.size() * sizeof(int32_t));
+  if (ids && !C.empty()) std::memcpy(ids, C.data(), C.size() * sizeof(int32_t));
+  return SP_SUCCESS;
+}
+
+sp_status sp_ogs_gather_scatter(const sp_ogs_plan* p, sp_type type, sp_op op, sp_transpose trans,
+                                int32_t k, void* v, sp_stream_t stream) {
+  sp_status st = check_common(p, type, op, trans, k, "sp_ogs_gather_scatter");
+  if (st) return st;
+  if (p->nnzT > 0 && !v) return fail(SP_ERR_INVALID_ARG, "sp_ogs_gather_scatter: null vector");
+  if (p->NrowBlocksT == 0) return SP_SUCCESS;
+  cudaStream_t s = as_cuda(stream);
+  switch (type) {
+    case SP_FLOAT: by_op<GsF, float>(op, p, trans, (int)k, v, s); break;
+    case SP_DOUBLE: by_op<GsF, double>(op, p, trans, (int)k, v, s); break;
+    case SP_INT32: by_op<GsF, int32_t>(op, p, trans, (int)k, v, s); break;
+    case SP_INT64: by_op<GsF, long long>(op, p, trans, (int)k, v, s); break;
+  }
+  return check_launch("sp_ogs_gather_scatter");
+}
+
+sp_status sp_ogs_gather(const sp_ogs_plan* p, sp_type type, sp_op op, sp_transpose trans,
+                        int32_t k, void* gv, const void* v, sp_stream_t stream) {
+  sp_status st = check_common(p, type, op, trans, k, "sp_ogs_gather");
+  if (st) return st;
+  const int32_t nb = (trans == SP_NOTRANS) ? p->NrowBlocksN : p->NrowBlocksT;
+  if (nb == 0) return SP_SUCCESS;
+  if (!v || !gv) return fail(SP_ERR_INVALID_ARG, "sp_ogs_gather: null vector");
+  cudaStream_t s = as_cuda(stream);
+  switch (type) {
+    case SP_FLOAT: by_op<GatherF, float>(op, p, trans, (int)k, gv, v, s); break;
+    case SP_DOUBLE: by_op<GatherF, double>(op, p, trans, (int)k, gv, v, s); break;
+    case SP_INT32: by_op<GatherF, int32_t>(op, p, trans, (int)k, gv, v, s); break;
+    case SP_INT64: by_op<GatherF, long long>(op, p, trans, (int)k, gv, v, s); break;
+  }
+  return check_launch("sp_ogs_gather");
+}
+
+sp_status sp_ogs_scatter(const sp_ogs_plan* p, sp_type type, sp_transpose trans, int32_t k,
+                         void* v, const void* gv, sp_stream_t stream) {
+  sp_status st = check_common(p, type, SP_OP_ADD, trans, k, "sp_ogs_scatter");
+  if (st) return st;
+  const int32_t nb = (trans == SP_TRANS) ? p->NrowBlocksN : p->NrowBlocksT;
+  if (nb == 0) return SP_SUCCESS;
+  if (!v || !gv) return fail(SP_ERR_INVALID_ARG, "sp_ogs_scatter: null vector");
+  cudaStream_t s = as_cuda(stream);
+  switch (type) {
+    case SP_FLOAT: launch_scatter<float>(p, trans, k, (float*)v, (const float*)gv, s); break;
+    case SP_DOUBLE: launch_scatter<double>(p, trans, k, (double*)v, (const double*)gv, s); break;
+    case SP_INT32: launch_scatter<int32_t>(p, trans, k, (int32_t*)v, (const int32_t*)gv, s); break;
+    case SP_INT64:
+      launch_scatter<long long>(p, trans, k, (long long*)v, (const long long*)gv, s);
+      break;
+  }
+  return check_launch("sp_ogs_scatter");
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// Device-resident gather-scatter plan (the local ogsOperator_t of one rank).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "sp_internal.h"
+
+namespace sp {
+
+// Largest number of non-zeros one thread block stages (8 per lane of 256 lanes).
+constexpr int kOgsThreads  = 256;
+constexpr int kOgsPerLane  = 8;
+constexpr int kOgsBlockNnz = kOgsThreads * kOgsPerLane;   // 2048
+// The reference refuses groups larger than this (libs/ogs/ogsOperator.cpp:535).
+constexpr int kOgsMaxRowSize = 512;
+
+struct OgsOperatorDev {
+  int32_t nrows = 0;       // rows covered by `blocks`
+  int32_t nblocks = 0;
+  int32_t* rowStarts = nullptr;  // nrows_padded + 1
+  int32_t* colIds = nullptr;     // nnz
+  int32_t* blocks = nullptr;     // nblocks + 1 row offsets
+};
+
+// Greedy partition of rows into blocks of at most kOgsBlockNnz non-zeros and at
+// most kOgsBlockNnz rows.  Returns false when one row alone is too large.
+bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t>& blocks);
+
+}  // namespace sp
+
+struct sp_ogs_plan {
+  int32_t N = 0;
+  int32_t NrowsT = 0, NrowsN = 0;
+  int32_t nnzT = 0, nnzN = 0;
+  int32_t maxRowSize = 0;
+  bool n_is_t = false;            // N operator shares T's arrays
+
+  std::vector<int32_t> rowStartsT, colIdsT;   // host copies, NrowsT+1 / nnzT
+  std::vector<int32_t> rowStartsN, colIdsN;   // host copies, NrowsN+1 / nnzN
+
+  // device arrays
+  int32_t* d_rowStartsT = nullptr;   // NrowsT + 1
+  int32_t* d_colIdsT = nullptr;      // nnzT
+  int32_t* d_rowStartsNpad = nullptr;// NrowsT + 1 (rows >= NrowsN empty)
+  int32_t* d_colIdsN = nullptr;      // nnzN
+  int32_t* d_blocksT = nullptr;      // partition of T rows by T non-zeros
+  int32_t* d_blocksN = nullptr;      // partition of N rows [0, NrowsN) by N non-zeros
+  int32_t NrowBlocksT = 0, NrowBlocksN = 0;
+  bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
+  bool own_blocks_n = false;      // d_blocksN is a separate allocation
+
+  int device = 0;
+};

@@ -1,0 +1,68 @@
+// Library-wide utilities: error strings, launch counter, BS0 graph objects.
+#include <cstdarg>
+#include <mutex>
+#include <vector>
+
+#include "sp_internal.h"
+
+namespace sp {
+
+static thread_local std::string t_last_error;
+static thread_local int64_t t_launches = 0;
+
+sp_status fail(sp_status s, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+  return s;
+}
+
+void clear_error() { t_last_error.clear(); }
+void count_launch(int64_t n) { t_launches += n; }
+
+int sm_count() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+}  // namespace sp
+
+extern "C" {
+
+const char* sp_last_error_string(void) { return sp::t_last_error.c_str(); }
+
+const char* sp_status_string(sp_status s) {
+  switch (s) {
+    case SP_SUCCESS: return "success";
+    case SP_ERR_INVALID_ARG: return "invalid argument";
+    case SP_ERR_CUDA: return "CUDA error";
+    case SP_ERR_ALLOC: return "allocation failed";
+    case SP_ERR_UNSUPPORTED: return "unsupported combination";
+    case SP_ERR_SIZE: return "size limit exceeded";
+    case SP_ERR_CSR: return "malformed CSR or ids";
+    case SP_ERR_TIMEOUT: return "device wait timed out";
+    case SP_ERR_DEVICE_CHECK: return "device bounds check failed";
+    default: return "unknown status";
+  }
+}
+
+int32_t sp_version(void) { return 100; }  // 0.1.0
+
+int64_t sp_launch_count(void) { return sp::t_launches; }
+void sp_launch_count_reset(void) { sp::t_launches = 0; }
+
+}  // extern "C"

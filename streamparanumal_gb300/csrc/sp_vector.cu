@@ -1,0 +1,790 @@
+// BS0-BS5 streaming kernels for sm_103a.
+//
+// All FP64 arithmetic is written with explicit fma()/add so the rounding is fixed
+// by the source, not by the compiler's contraction choices.  The choices follow
+// the reference's CUDA mode, which compiles OKL with --fmad=true
+// (libs/core/platformProperties.cpp:76):
+//   bs2:  alpha*x + beta*y   -> fma(alpha, x, beta*y)
+//   bs3:  acc += a*a         -> fma(a, a, acc)
+//   bs4:  acc += a*b         -> fma(a, b, acc)
+//   bs5:  r + alpha*Ap       -> fma(alpha, Ap, r);  acc += r*r -> fma(r, r, acc)
+#include <cstdint>
+#include <initializer_list>
+
+#include "sp_internal.h"
+
+namespace sp {
+
+// ------------------------------------------------------------------ helpers
+
+template <typename T> struct Vec16;
+template <> struct Vec16<double> { using type = double2; static constexpr int W = 2; };
+template <> struct Vec16<float>  { using type = float4;  static constexpr int W = 4; };
+
+__device__ __forceinline__ double2 vload(const double2* p) { return __ldcs(p); }
+__device__ __forceinline__ float4  vload(const float4* p)  { return __ldcs(p); }
+__device__ __forceinline__ void vstore(double2* p, double2 v) { __stcs(p, v); }
+__device__ __forceinline__ void vstore(float4* p, float4 v)   { __stcs(p, v); }
+
+static inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Grid for a "U vectors of 16 bytes per thread" streaming kernel.
+static inline unsigned stream_grid(int64_t nvec, int threads, int U) {
+  int64_t per = (int64_t)threads * U;
+  int64_t g = (nvec + per - 1) / per;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+// ------------------------------------------------------------------ BS0
+
+__global__ void k_bs0(int n, const double* __restrict__ a, double* __restrict__ b) {
+  (void)a;
+  // one block, one thread: the store happens only when n == 0 (bs0.okl:33-35)
+  if ((int)threadIdx.x == n && (int)blockIdx.x == n) b[0] = 0.0;
+}
+
+// ------------------------------------------------------------------ BS1 copy
+
+constexpr int kStreamThreads = 256;
+
+template <typename T, int U>
+__global__ void __launch_bounds__(kStreamThreads)
+k_copy_vec(const typename Vec16<T>::type* __restrict__ a, typename Vec16<T>::type* __restrict__ b,
+           int64_t nvec, const T* __restrict__ as, T* __restrict__ bs, int64_t n) {
+  using V = typename Vec16<T>::type;
+  const int64_t base = (int64_t)blockIdx.x * (kStreamThreads * U) + threadIdx.x;
+  V v[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kStreamThreads;
+    if (i < nvec) v[u] = vload(a + i);
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kStreamThreads;
+    if (i < nvec) vstore(b + i, v[u]);
+  }
+  // scalar tail (fewer than one vector)
+  if (blockIdx.x == 0) {
+    const int64_t t = nvec * Vec16<T>::W + threadIdx.x;
+    if (t < n) bs[t] = as[t];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kStreamThreads)
+k_copy_scalar(const T* __restrict__ a, T* __restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+template <typename T>
+static sp_status launch_copy(int64_t n, const T* a, T* b, cudaStream_t s, const char* name) {
+  if (n < 0) return fail(SP_ERR_INVALID_ARG, "%s: negative length %lld", name, (long long)n);
+  if (n == 0) return SP_SUCCESS;
+  if (!a || !b) return fail(SP_ERR_INVALID_ARG, "%s: null pointer", name);
+  constexpr int W = Vec16<T>::W;
+  if (aligned16(a) && aligned16(b)) {
+    constexpr int U = 4;
+    const int64_t nvec = n / W;
+    k_copy_vec<T, U><<<stream_grid(nvec, kStreamThreads, U), kStreamThreads, 0, s>>>(
+        reinterpret_cast<const typename Vec16<T>::type*>(a),
+        reinterpret_cast<typename Vec16<T>::type*>(b), nvec, a, b, n);
+  } else {
+    k_copy_scalar<T><<<stream_grid(n, kStreamThreads, 4), kStreamThreads, 0, s>>>(a, b, n);
+  }
+  return check_launch(name);
+}
+
+// ------------------------------------------------------------------ BS2 axpy
+
+__device__ __forceinline__ double axpby(double al, double x, double be, double y) {
+  return fma(al, x, be * y);
+}
+__device__ __forceinline__ float axpby(float al, float x, float be, float y) {
+  return fmaf(al, x, be * y);
+}
+__device__ __forceinline__ double2 axpby(double al, double2 x, double be, double2 y) {
+  return make_double2(axpby(al, x.x, be, y.x), axpby(al, x.y, be, y.y));
+}
+__device__ __forceinline__ float4 axpby(float al, float4 x, float be, float4 y) {
+  return make_float4(axpby(al, x.x, be, y.x), axpby(al, x.y, be, y.y), axpby(al, x.z, be, y.z),
+                     axpby(al, x.w, be, y.w));
+}
+
+template <typename T, int U>
+__global__ void __launch_bounds__(kStreamThreads)
+k_axpy_vec(int64_t nvec, T alpha, const typename Vec16<T>::type* __restrict__ x, T beta,
+           typename Vec16<T>::type* __restrict__ y, const T* __restrict__ xs, T* __restrict__ ys,
+           int64_t n) {
+  using V = typename Vec16<T>::type;
+  const int64_t base = (int64_t)blockIdx.x * (kStreamThreads * U) + threadIdx.x;
+  V vx[U], vy[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kStreamThreads;
+    if (i < nvec) { vx[u] = vload(x + i); vy[u] = vload(y + i); }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kStreamThreads;
+    if (i < nvec) vstore(y + i, axpby(alpha, vx[u], beta, vy[u]));
+  }
+  if (blockIdx.x == 0) {
+    const int64_t t = nvec * Vec16<T>::W + threadIdx.x;
+    if (t < n) ys[t] = axpby(alpha, xs[t], beta, ys[t]);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kStreamThreads)
+k_axpy_scalar(int64_t n, T alpha, const T* __restrict__ x, T beta, T* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = axpby(alpha, x[i], beta, y[i]);
+}
+
+template <typename T>
+static sp_status launch_axpy(int64_t n, T alpha, const T* x, T beta, T* y, cudaStream_t s,
+                             const char* name) {
+  if (n < 0) return fail(SP_ERR_INVALID_ARG, "%s: negative length %lld", name, (long long)n);
+  if (n == 0) return SP_SUCCESS;
+  if (!x || !y) return fail(SP_ERR_INVALID_ARG, "%s: null pointer", name);
+  constexpr int W = Vec16<T>::W;
+  if (aligned16(x) && aligned16(y)) {
+    constexpr int U = 4;
+    const int64_t nvec = n / W;
+    k_axpy_vec<T, U><<<stream_grid(nvec, kStreamThreads, U), kStreamThreads, 0, s>>>(
+        nvec, alpha, reinterpret_cast<const typename Vec16<T>::type*>(x), beta,
+        reinterpret_cast<typename Vec16<T>::type*>(y), x, y, n);
+  } else {
+    k_axpy_scalar<T><<<stream_grid(n, kStreamThreads, 4), kStreamThreads, 0, s>>>(n, alpha, x,
+                                                                                   beta, y);
+  }
+  return check_launch(name);
+}
+
+// ------------------------------------------------------------------ order-exact reductions
+//
+// The halving tree of the reference's reduction kernels (bs3.okl:43-63 and the
+// identical trees of bs4/bs5): level h adds s[t+h] into s[t] for t < h, for
+// h = BS/2 ... 2, and the result is s[0] + s[1].  Levels h >= 64 run through
+// shared memory; h = 32 ... 1 run in warp 0 with shuffles, which performs the
+// same additions on the same operands.
+template <int BS>
+__device__ __forceinline__ double tree_reduce(double v, double* s) {
+  const int t = threadIdx.x;
+  s[t] = v;
+  __syncthreads();
+#pragma unroll
+  for (int h = BS / 2; h >= 64; h >>= 1) {
+    if (t < h) s[t] = s[t] + s[t + h];
+    __syncthreads();
+  }
+  double r = 0.0;
+  if (t < 32) {
+    r = s[t] + s[t + 32];
+    r = r + __shfl_down_sync(0xffffffffu, r, 16);
+    r = r + __shfl_down_sync(0xffffffffu, r, 8);
+    r = r + __shfl_down_sync(0xffffffffu, r, 4);
+    r = r + __shfl_down_sync(0xffffffffu, r, 2);
+    r = r + __shfl_down_sync(0xffffffffu, r, 1);
+  }
+  return r;  // valid in thread 0
+}
+
+// Lane t of logical block b visits t + b*BS + j*BS*nblocks for j = 0, 1, ...
+// (bs3.okl:36-41).  U loads are issued ahead of the in-order accumulation.
+template <int BS, int U>
+__global__ void __launch_bounds__(BS)
+k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict__ partial) {
+  __shared__ double s[BS];
+  const int64_t stride = (int64_t)BS * nblocks;
+  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  double acc = 0.0;
+  for (; id + (U - 1) * stride < n; id += U * stride) {
+    double v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = __ldcs(a + id + u * stride);
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = fma(v[u], v[u], acc);
+  }
+  for (; id < n; id += stride) {
+    const double v = __ldcs(a + id);
+    acc = fma(v, v, acc);
+  }
+  const double r = tree_reduce<BS>(acc, s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+template <int BS, int U>
+__global__ void __launch_bounds__(BS)
+k_bs4_1(int nblocks, int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+        double* __restrict__ partial) {
+  __shared__ double s[BS];
+  const int64_t stride = (int64_t)BS * nblocks;
+  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  double acc = 0.0;
+  for (; id + (U - 1) * stride < n; id += U * stride) {
+    double va[U], vb[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      va[u] = __ldcs(a + id + u * stride);
+      vb[u] = __ldcs(b + id + u * stride);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = fma(va[u], vb[u], acc);
+  }
+  for (; id < n; id += stride) acc = fma(__ldcs(a + id), __ldcs(b + id), acc);
+  const double r = tree_reduce<BS>(acc, s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+template <int BS, int U>
+__global__ void __launch_bounds__(BS)
+k_bs5_1(int nblocks, int64_t n, const double* __restrict__ Ap, double alpha, double* __restrict__ r,
+        double* __restrict__ partial) {
+  __shared__ double s[BS];
+  const int64_t stride = (int64_t)BS * nblocks;
+  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  double acc = 0.0;
+  for (; id + (U - 1) * stride < n; id += U * stride) {
+    double vr[U], va[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      vr[u] = __ldcs(r + id + u * stride);
+      va[u] = __ldcs(Ap + id + u * stride);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const double rr = fma(alpha, va[u], vr[u]);
+      __stcs(r + id + u * stride, rr);
+      acc = fma(rr, rr, acc);
+    }
+  }
+  for (; id < n; id += stride) {
+    const double rr = fma(alpha, __ldcs(Ap + id), __ldcs(r + id));
+    __stcs(r + id, rr);
+    acc = fma(rr, rr, acc);
+  }
+  const double res = tree_reduce<BS>(acc, s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = res;
+}
+
+// Stage 2 (bs3.okl:66-102): lane t holds 0.0 + partial[t] (t < nblocks, each lane
+// sees at most one entry because the stride BS*nblocks >= nblocks), then the tree.
+template <int BS>
+__global__ void __launch_bounds__(BS)
+k_finish(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
+  __shared__ double s[BS];
+  const int t = threadIdx.x;
+  double v = 0.0;
+  if (t < nblocks) v = 0.0 + partial[t];
+  const double r = tree_reduce<BS>(v, s);
+  if (t == 0) out[0] = r;
+}
+
+static sp_status check_exact_args(int32_t bs, int32_t nblocks, int64_t n, const char* name) {
+  if (bs != 256 && bs != 512 && bs != 1024)
+    return fail(SP_ERR_INVALID_ARG, "%s: block_size %d not in {256,512,1024}", name, bs);
+  if (nblocks < 1 || nblocks > bs)
+    return fail(SP_ERR_INVALID_ARG, "%s: nblocks %d outside [1, %d]", name, nblocks, bs);
+  if (n < 0) return fail(SP_ERR_INVALID_ARG, "%s: negative length", name);
+  return SP_SUCCESS;
+}
+
+// ------------------------------------------------------------------ single-launch reductions
+//
+// Fixed grid of G blocks; lane accumulation over a grid-stride loop, block tree,
+// per-block partial to scratch, and the last block to arrive (ticket counter)
+// reduces the G partials in a fixed order and resets the counter to zero.
+
+constexpr int kRedThreads = 256;
+
+struct RedScratch {
+  unsigned int* ticket;
+  double* partial;  // 2*kMaxRedBlocks doubles
+};
+
+__host__ __device__ inline RedScratch red_scratch(void* p) {
+  char* c = static_cast<char*>(p);
+  return RedScratch{reinterpret_cast<unsigned int*>(c),
+                    reinterpret_cast<double*>(c + kRedPartialOff)};
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) v += __shfl_down_sync(0xffffffffu, v, h);
+  return v;
+}
+
+// Sum of `v` over the block (result valid in thread 0), fixed order.
+__device__ __forceinline__ double block_sum(double v, double* s) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) s[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? s[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Writes the block's value, and lets the last block finish into out[0].
+__device__ __forceinline__ void finish_ticket(double block_val, RedScratch sc, double* out,
+                                              double* s) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    sc.partial[blockIdx.x] = block_val;
+    __threadfence();
+    const unsigned t = atomicAdd(sc.ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(sc.partial + i);
+  const double r = block_sum(v, s);
+  if (threadIdx.x == 0) {
+    out[0] = r;
+    *sc.ticket = 0u;  // leave the scratch zeroed for the next call
+  }
+}
+
+// Error-free transformation a + b = s + e (Knuth TwoSum), FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Compensated FP32 accumulation of a product (Ogita-Rump-Oishi Dot2 step).
+__device__ __forceinline__ void dot2_step(float a, float b, float& s, float& c) {
+  const float p = a * b;
+  const float pe = fmaf(a, b, -p);
+  float t, e;
+  two_sum(s, p, t, e);
+  s = t;
+  c += e + pe;
+}
+
+template <int U>
+__global__ void __launch_bounds__(kRedThreads)
+k_dot_f64_fast(int64_t nvec, const double2* __restrict__ a, const double2* __restrict__ b,
+               const double* __restrict__ as, const double* __restrict__ bs, int64_t n,
+               void* scratch, double* out) {
+  __shared__ double s[32];
+  const RedScratch sc = red_scratch(scratch);
+  double acc0 = 0.0, acc1 = 0.0;
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
+       base += step) {
+    double2 va[U], vb[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        va[u] = __ldcs(a + i);
+        vb[u] = (b == a) ? va[u] : __ldcs(b + i);
+      } else {
+        va[u] = make_double2(0.0, 0.0);
+        vb[u] = va[u];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      acc0 = fma(va[u].x, vb[u].x, acc0);
+      acc1 = fma(va[u].y, vb[u].y, acc1);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) acc0 = fma(as[n - 1], bs[n - 1], acc0);
+  const double bv = block_sum(acc0 + acc1, s);
+  finish_ticket(bv, sc, out, s);
+}
+
+template <int U>
+__global__ void __launch_bounds__(kRedThreads)
+k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restrict__ b,
+               const float* __restrict__ as, const float* __restrict__ bs, int64_t n,
+               void* scratch, double* out) {
+  __shared__ double s[32];
+  const RedScratch sc = red_scratch(scratch);
+  float sum = 0.f, comp = 0.f;
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
+       base += step) {
+    float4 va[U], vb[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        va[u] = __ldcs(a + i);
+        vb[u] = (b == a) ? va[u] : __ldcs(b + i);
+      } else {
+        va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vb[u] = va[u];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      dot2_step(va[u].x, vb[u].x, sum, comp);
+      dot2_step(va[u].y, vb[u].y, sum, comp);
+      dot2_step(va[u].z, vb[u].z, sum, comp);
+      dot2_step(va[u].w, vb[u].w, sum, comp);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int64_t t = nvec * 4; t < n; ++t) dot2_step(as[t], bs[t], sum, comp);
+  }
+  const double bv = block_sum((double)sum + (double)comp, s);
+  finish_ticket(bv, sc, out, s);
+}
+
+// x += alpha p ; r -= alpha Ap ; out = sum r*r     (FP64 storage)
+template <int U>
+__global__ void __launch_bounds__(kRedThreads)
+k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double2* __restrict__ Ap,
+         double2* __restrict__ x, double2* __restrict__ r, const double* __restrict__ ps,
+         const double* __restrict__ Aps, double* __restrict__ xs, double* __restrict__ rs,
+         int64_t n, void* scratch, double* out) {
+  __shared__ double s[32];
+  const RedScratch sc = red_scratch(scratch);
+  double acc0 = 0.0, acc1 = 0.0;
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
+       base += step) {
+    double2 vp[U], va[U], vx[U], vr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        vp[u] = __ldcs(p + i);
+        va[u] = __ldcs(Ap + i);
+        vx[u] = __ldcs(x + i);
+        vr[u] = __ldcs(r + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        double2 nx, nr;
+        nx.x = fma(alpha, vp[u].x, vx[u].x);
+        nx.y = fma(alpha, vp[u].y, vx[u].y);
+        nr.x = fma(-alpha, va[u].x, vr[u].x);
+        nr.y = fma(-alpha, va[u].y, vr[u].y);
+        __stcs(x + i, nx);
+        __stcs(r + i, nr);
+        acc0 = fma(nr.x, nr.x, acc0);
+        acc1 = fma(nr.y, nr.y, acc1);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
+    const int64_t t = n - 1;
+    xs[t] = fma(alpha, ps[t], xs[t]);
+    const double nr = fma(-alpha, Aps[t], rs[t]);
+    rs[t] = nr;
+    acc0 = fma(nr, nr, acc0);
+  }
+  const double bv = block_sum(acc0 + acc1, s);
+  finish_ticket(bv, sc, out, s);
+}
+
+// FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
+// r.r with compensated FP32 lanes and an FP64 cross-block finish.
+template <int U>
+__global__ void __launch_bounds__(kRedThreads)
+k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* __restrict__ Ap,
+         float4* __restrict__ x, float4* __restrict__ r, const float* __restrict__ ps,
+         const float* __restrict__ Aps, float* __restrict__ xs, float* __restrict__ rs, int64_t n,
+         void* scratch, double* out) {
+  __shared__ double s[32];
+  const RedScratch sc = red_scratch(scratch);
+  float sum = 0.f, comp = 0.f;
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
+       base += step) {
+    float4 vp[U], va[U], vx[U], vr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        vp[u] = __ldcs(p + i);
+        va[u] = __ldcs(Ap + i);
+        vx[u] = __ldcs(x + i);
+        vr[u] = __ldcs(r + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      if (i < nvec) {
+        float4 nx, nr;
+        nx.x = fmaf(alpha, vp[u].x, vx[u].x);
+        nx.y = fmaf(alpha, vp[u].y, vx[u].y);
+        nx.z = fmaf(alpha, vp[u].z, vx[u].z);
+        nx.w = fmaf(alpha, vp[u].w, vx[u].w);
+        nr.x = fmaf(-alpha, va[u].x, vr[u].x);
+        nr.y = fmaf(-alpha, va[u].y, vr[u].y);
+        nr.z = fmaf(-alpha, va[u].z, vr[u].z);
+        nr.w = fmaf(-alpha, va[u].w, vr[u].w);
+        __stcs(x + i, nx);
+        __stcs(r + i, nr);
+        dot2_step(nr.x, nr.x, sum, comp);
+        dot2_step(nr.y, nr.y, sum, comp);
+        dot2_step(nr.z, nr.z, sum, comp);
+        dot2_step(nr.w, nr.w, sum, comp);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int64_t t = nvec * 4; t < n; ++t) {
+      xs[t] = fmaf(alpha, ps[t], xs[t]);
+      const float nr = fmaf(-alpha, Aps[t], rs[t]);
+      rs[t] = nr;
+      dot2_step(nr, nr, sum, comp);
+    }
+  }
+  const double bv = block_sum((double)sum + (double)comp, s);
+  finish_ticket(bv, sc, out, s);
+}
+
+static unsigned red_grid(int64_t nvec, int U) {
+  int64_t per = (int64_t)kRedThreads * U;
+  int64_t g = (nvec + per - 1) / per;
+  int64_t cap = 8 * (int64_t)sm_count();
+  if (cap > kMaxRedBlocks) cap = kMaxRedBlocks;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+static sp_status check_red_args(int64_t n, const void* scratch, const void* out,
+                                std::initializer_list<const void*> vecs, const char* name) {
+  if (n < 0) return fail(SP_ERR_INVALID_ARG, "%s: negative length", name);
+  if (!scratch || !out) return fail(SP_ERR_INVALID_ARG, "%s: null scratch/out", name);
+  if (reinterpret_cast<uintptr_t>(scratch) & 255u)
+    return fail(SP_ERR_INVALID_ARG, "%s: scratch must be 256-byte aligned", name);
+  for (const void* v : vecs) {
+    if (n > 0 && !v) return fail(SP_ERR_INVALID_ARG, "%s: null vector", name);
+    if (n > 0 && !aligned16(v))
+      return fail(SP_ERR_INVALID_ARG, "%s: vectors must be 16-byte aligned", name);
+  }
+  return SP_SUCCESS;
+}
+
+}  // namespace sp
+
+using namespace sp;
+
+extern "C" {
+
+sp_status sp_bs0(int32_t n, const double* a, double* b, sp_stream_t stream) {
+  if (!b && n == 0) return fail(SP_ERR_INVALID_ARG, "sp_bs0: null output with n == 0");
+  k_bs0<<<1, 1, 0, as_cuda(stream)>>>(n, a, b);
+  return check_launch("sp_bs0");
+}
+
+sp_status sp_bs1_copy_f64(int64_t n, const double* a, double* b, sp_stream_t stream) {
+  return launch_copy<double>(n, a, b, as_cuda(stream), "sp_bs1_copy_f64");
+}
+sp_status sp_bs1_copy_f32(int64_t n, const float* a, float* b, sp_stream_t stream) {
+  return launch_copy<float>(n, a, b, as_cuda(stream), "sp_bs1_copy_f32");
+}
+
+sp_status sp_bs2_axpy_f64(int64_t n, double alpha, const double* x, double beta, double* y,
+                          sp_stream_t stream) {
+  return launch_axpy<double>(n, alpha, x, beta, y, as_cuda(stream), "sp_bs2_axpy_f64");
+}
+sp_status sp_bs2_axpy_f32(int64_t n, float alpha, const float* x, float beta, float* y,
+                          sp_stream_t stream) {
+  return launch_axpy<float>(n, alpha, x, beta, y, as_cuda(stream), "sp_bs2_axpy_f32");
+}
+
+sp_status sp_bs3_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, double* partial,
+                       sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs3_1_f64");
+  if (st) return st;
+  if (!partial || (n > 0 && !a)) return fail(SP_ERR_INVALID_ARG, "sp_bs3_1_f64: null pointer");
+  cudaStream_t s = as_cuda(stream);
+  if (bs == 256) k_bs3_1<256, 16><<<nblocks, 256, 0, s>>>(nblocks, n, a, partial);
+  else if (bs == 512) k_bs3_1<512, 8><<<nblocks, 512, 0, s>>>(nblocks, n, a, partial);
+  else k_bs3_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, partial);
+  return check_launch("sp_bs3_1_f64");
+}
+
+sp_status sp_bs4_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, const double* b,
+                       double* partial, sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs4_1_f64");
+  if (st) return st;
+  if (!partial || (n > 0 && (!a || !b)))
+    return fail(SP_ERR_INVALID_ARG, "sp_bs4_1_f64: null pointer");
+  cudaStream_t s = as_cuda(stream);
+  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial);
+  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial);
+  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial);
+  return check_launch("sp_bs4_1_f64");
+}
+
+sp_status sp_bs5_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* Ap, double alpha,
+                       double* r, double* partial, sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs5_1_f64");
+  if (st) return st;
+  if (!partial || (n > 0 && (!Ap || !r)))
+    return fail(SP_ERR_INVALID_ARG, "sp_bs5_1_f64: null pointer");
+  cudaStream_t s = as_cuda(stream);
+  if (bs == 256) k_bs5_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
+  else if (bs == 512) k_bs5_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
+  else k_bs5_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
+  return check_launch("sp_bs5_1_f64");
+}
+
+sp_status sp_reduce_finish_f64(int32_t bs, int32_t nblocks, const double* partial, double* out,
+                               sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, 0, "sp_reduce_finish_f64");
+  if (st) return st;
+  if (!partial || !out) return fail(SP_ERR_INVALID_ARG, "sp_reduce_finish_f64: null pointer");
+  cudaStream_t s = as_cuda(stream);
+  if (bs == 256) k_finish<256><<<1, 256, 0, s>>>(nblocks, partial, out);
+  else if (bs == 512) k_finish<512><<<1, 512, 0, s>>>(nblocks, partial, out);
+  else k_finish<1024><<<1, 1024, 0, s>>>(nblocks, partial, out);
+  return check_launch("sp_reduce_finish_f64");
+}
+
+size_t sp_reduce_scratch_bytes(void) { return kRedScratchSize; }
+
+sp_status sp_dot_f64(int64_t n, const double* a, const double* b, double* out, void* scratch,
+                     sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, out, {a, b}, "sp_dot_f64");
+  if (st) return st;
+  constexpr int U = 4;
+  const int64_t nvec = n / 2;
+  k_dot_f64_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, reinterpret_cast<const double2*>(a), reinterpret_cast<const double2*>(b), a, b, n,
+      scratch, out);
+  return check_launch("sp_dot_f64");
+}
+
+sp_status sp_norm2_f64(int64_t n, const double* a, double* out, void* scratch,
+                       sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, out, {a}, "sp_norm2_f64");
+  if (st) return st;
+  constexpr int U = 4;
+  const int64_t nvec = n / 2;
+  k_dot_f64_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, reinterpret_cast<const double2*>(a), reinterpret_cast<const double2*>(a), a, a, n,
+      scratch, out);
+  return check_launch("sp_norm2_f64");
+}
+
+sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, void* scratch,
+                     sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, out, {a, b}, "sp_dot_f32");
+  if (st) return st;
+  constexpr int U = 4;
+  const int64_t nvec = n / 4;
+  k_dot_f32_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b), a, b, n,
+      scratch, out);
+  return check_launch("sp_dot_f32");
+}
+
+sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch,
+                       sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, out, {a}, "sp_norm2_f32");
+  if (st) return st;
+  constexpr int U = 4;
+  const int64_t nvec = n / 4;
+  k_dot_f32_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(a), a, a, n,
+      scratch, out);
+  return check_launch("sp_norm2_f32");
+}
+
+sp_status sp_cg_update_f64(int64_t n, double alpha, const double* p, const double* Ap, double* x,
+                           double* r, double* rdotr, void* scratch, sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, rdotr, {p, Ap, x, r}, "sp_cg_update_f64");
+  if (st) return st;
+  constexpr int U = 2;
+  const int64_t nvec = n / 2;
+  k_cg_f64<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, alpha, reinterpret_cast<const double2*>(p), reinterpret_cast<const double2*>(Ap),
+      reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), p, Ap, x, r, n, scratch,
+      rdotr);
+  return check_launch("sp_cg_update_f64");
+}
+
+sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float* Ap, float* x,
+                           float* r, double* rdotr, void* scratch, sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, rdotr, {p, Ap, x, r}, "sp_cg_update_f32");
+  if (st) return st;
+  constexpr int U = 2;
+  const int64_t nvec = n / 4;
+  k_cg_f32<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, (float)alpha, reinterpret_cast<const float4*>(p), reinterpret_cast<const float4*>(Ap),
+      reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r), p, Ap, x, r, n, scratch, rdotr);
+  return check_launch("sp_cg_update_f32");
+}
+
+// ------------------------------------------------------------------ BS0 graph form
+
+}  // extern "C"
+
+struct sp_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int32_t nlaunches = 0;
+};
+
+extern "C" {
+
+sp_status sp_bs0_graph_create(int32_t nlaunches, int32_t n, const double* a, double* b,
+                              sp_stream_t stream, sp_graph** out) {
+  if (!out || nlaunches < 1) return fail(SP_ERR_INVALID_ARG, "sp_bs0_graph_create: bad args");
+  if (!b && n == 0) return fail(SP_ERR_INVALID_ARG, "sp_bs0_graph_create: null output");
+  *out = nullptr;
+  cudaStream_t cap = nullptr;
+  SP_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  sp_graph* g = new sp_graph();
+  g->nlaunches = nlaunches;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    for (int i = 0; i < nlaunches; ++i) k_bs0<<<1, 1, 0, cap>>>(n, a, b);
+    e = cudaStreamEndCapture(cap, &g->graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e == cudaSuccess) e = cudaGraphUpload(g->exec, as_cuda(stream));
+  cudaStreamDestroy(cap);
+  if (e != cudaSuccess) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return fail(SP_ERR_CUDA, "sp_bs0_graph_create: %s", cudaGetErrorString(e));
+  }
+  *out = g;
+  return SP_SUCCESS;
+}
+
+sp_status sp_graph_launch(const sp_graph* g, sp_stream_t stream) {
+  if (!g || !g->exec) return fail(SP_ERR_INVALID_ARG, "sp_graph_launch: null graph");
+  SP_CUDA_TRY(cudaGraphLaunch(g->exec, as_cuda(stream)));
+  count_launch(g->nlaunches);
+  return SP_SUCCESS;
+}
+
+sp_status sp_graph_destroy(sp_graph* g) {
+  if (!g) return SP_SUCCESS;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return SP_SUCCESS;
+}
+
+}  // extern "C"

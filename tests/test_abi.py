@@ -1,0 +1,106 @@
+"""The C ABI library loads and exports every entry point of include/*.h; argument
+validation returns the documented status before any device work (CPU only)."""
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+from streamparanumal_gb300 import capi
+
+
+def test_every_declared_function_is_exported(lib):
+    declared = capi.header_functions()
+    assert len(declared) >= 30
+    out = subprocess.run(["nm", "-D", "--defined-only", str(capi.LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [f for f in declared if f not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for f in declared:
+        assert hasattr(lib, f)
+    assert set(declared) == set(capi.SIGNATURES), "ctypes signatures out of sync with header"
+
+
+def test_build_targets_sm_103a_only():
+    from streamparanumal_gb300 import _build
+    assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_status_strings(lib):
+    assert lib.sp_status_string(0) == b"success"
+    assert lib.sp_status_string(capi.SP_ERR_CSR) == b"malformed CSR or ids"
+    assert lib.sp_version() == 100
+    assert lib.sp_ogs_block_nnz() == 2048
+    assert lib.sp_reduce_scratch_bytes() >= 256 + 16 * 1024
+
+
+@pytest.mark.parametrize("fn,args", [
+    ("sp_bs1_copy_f64", (-1, None, None, None)),
+    ("sp_bs2_axpy_f64", (-5, 1.0, None, 1.0, None, None)),
+    ("sp_bs3_1_f64", (100, 1, 10, None, None, None)),        # bad block size
+    ("sp_bs3_1_f64", (256, 0, 10, None, None, None)),        # nblocks < 1
+    ("sp_bs3_1_f64", (256, 257, 10, None, None, None)),      # nblocks > bs
+    ("sp_reduce_finish_f64", (1024, 2000, None, None, None)),
+    ("sp_norm2_f64", (10, None, None, None, None)),          # null scratch
+    ("sp_ogs_gather_scatter", (None, 1, 0, 0, 1, None, None)),  # null plan
+    ("sp_ogs_gather", (None, 1, 0, 0, 1, None, None, None)),
+    ("sp_ogs_scatter", (None, 1, 0, 1, None, None, None)),
+    ("sp_mesh_box_hex_ids", (0, 1, 1, 1, 0, None)),
+])
+def test_invalid_arguments_are_rejected_without_device_work(lib, fn, args):
+    st = capi.status(fn, *args)
+    assert st == capi.SP_ERR_INVALID_ARG
+    assert capi.last_error()
+
+
+def test_zero_length_is_a_no_op(lib):
+    assert capi.status("sp_bs1_copy_f64", 0, None, None, None) == 0
+    assert capi.status("sp_bs2_axpy_f32", 0, 1.0, None, 2.0, None, None) == 0
+
+
+def _plan_status(N, rs, ci, rsN=None, ciN=None):
+    h = ctypes.c_void_p()
+    rs = np.ascontiguousarray(rs, dtype=np.int32)
+    ci = np.ascontiguousarray(ci if len(ci) else [0], dtype=np.int32)
+    if rsN is None:
+        return capi.status("sp_ogs_plan_create", N, rs.size - 1, capi.i32p(rs), capi.i32p(ci),
+                           rs.size - 1, None, None, None, ctypes.byref(h))
+    rsN = np.ascontiguousarray(rsN, dtype=np.int32)
+    ciN = np.ascontiguousarray(ciN if len(ciN) else [0], dtype=np.int32)
+    return capi.status("sp_ogs_plan_create", N, rs.size - 1, capi.i32p(rs), capi.i32p(ci),
+                       rsN.size - 1, capi.i32p(rsN), capi.i32p(ciN), None, ctypes.byref(h))
+
+
+def test_plan_validation_rejects_malformed_csr(lib):
+    # rowStarts[0] != 0
+    assert _plan_status(4, [1, 2], [0]) == capi.SP_ERR_CSR
+    # not monotone
+    assert _plan_status(4, [0, 2, 1], [0, 1]) == capi.SP_ERR_CSR
+    # column out of range
+    assert _plan_status(4, [0, 1], [4]) == capi.SP_ERR_CSR
+    # one column in two rows
+    assert _plan_status(4, [0, 1, 2], [3, 3]) == capi.SP_ERR_CSR
+    # N member outside its T row
+    assert _plan_status(4, [0, 2, 4], [0, 1, 2, 3], [0, 1, 2], [2, 0]) == capi.SP_ERR_CSR
+    # NrowsN > NrowsT
+    assert _plan_status(4, [0, 1], [0], [0, 0, 0], []) == capi.SP_ERR_CSR
+
+
+def test_plan_validation_rejects_oversized_group(lib):
+    # the reference aborts on multiplicity > 512 (libs/ogs/ogsOperator.cpp:535)
+    n = 513
+    st = _plan_status(n, [0, n], np.arange(n))
+    assert st == capi.SP_ERR_SIZE
+    assert "Multiplicity" in capi.last_error()
+
+
+def test_unique_with_unsigned_kind_is_invalid(lib):
+    ids = np.arange(1, 5, dtype=np.int64)
+    z = np.zeros(8, dtype=np.int32)
+    nT, nN = ctypes.c_int32(), ctypes.c_int32()
+    st = capi.status("sp_ogs_setup_csr", 4, capi.i64p(ids), capi.UNSIGNED, 1,
+                     ctypes.byref(nT), capi.i32p(z), capi.i32p(z), ctypes.byref(nN),
+                     capi.i32p(z), capi.i32p(z))
+    assert st == capi.SP_ERR_INVALID_ARG
+    assert capi.last_error() == "Invalid ogs setup requested"

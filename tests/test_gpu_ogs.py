@@ -1,0 +1,182 @@
+"""ogs gather / scatter / gather+scatter kernels against the oracle's host loops
+(GPU).  Every type, op and transpose is bit-exact: sums run in CSR order from the
+op's identity, exactly as ogsOperator_t's loops do."""
+import numpy as np
+import pytest
+import torch
+
+from streamparanumal_gb300 import capi
+from streamparanumal_gb300 import ogs as O
+
+pytestmark = pytest.mark.gpu
+
+NP_TYPES = {capi.FLOAT: np.float32, capi.DOUBLE: np.float64, capi.INT32: np.int32,
+            capi.INT64: np.int64}
+
+
+def values(orc, n, dtype, seed):
+    u = orc.uniform(n, seed)
+    if dtype in (np.float32, np.float64):
+        return u.astype(dtype)
+    return np.round(u * 1000).astype(dtype)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def pad(rs, nrows):
+    return np.concatenate([rs, np.full(nrows + 1 - rs.size, rs[-1], rs.dtype)])
+
+
+def make(orc, ids, kind=capi.SIGNED, unique=True):
+    ids_o = ids.copy()
+    ref = orc.ogs_setup(ids_o, kind=kind, unique=unique)
+    h = O.ogs_t()
+    ids_p = ids.copy()
+    h.Setup(ids.size, ids_p, kind=kind, unique=unique)
+    rsT, ciT = h.csr(O.Trans)
+    np.testing.assert_array_equal(rsT, ref["rsT"])
+    np.testing.assert_array_equal(ciT, ref["ciT"])
+    return h, ref
+
+
+BOXES = [(2, 2, 2, 1, 0), (3, 2, 2, 3, 0), (4, 3, 2, 2, 99), (4, 4, 4, 7, 0), (5, 4, 3, 7, 2024),
+         (16, 16, 16, 7, 0)]
+
+
+@pytest.mark.parametrize("box", BOXES)
+def test_box_gather_scatter_sym_fp64(cuda, orc, box):
+    nx, ny, nz, p, seed = box
+    ids = O.box_hex_ids(nx, ny, nz, p, seed)
+    h, ref = make(orc, ids)
+    q = orc.uniform(ids.size, 17)
+    dq = torch.from_numpy(q).cuda()
+    h.GatherScatter(dq, 1, O.Add, O.Sym)
+    want = orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], q)
+    np.testing.assert_array_equal(host(dq), want)
+
+
+@pytest.mark.parametrize("box", BOXES)
+def test_box_gather_and_scatter_fp64(cuda, orc, box):
+    nx, ny, nz, p, seed = box
+    ids = O.box_hex_ids(nx, ny, nz, p, seed)
+    h, ref = make(orc, ids)
+    q = orc.uniform(ids.size, 23)
+    ng = ref["rsT"].size - 1
+    gq = torch.zeros(ng, dtype=torch.float64, device="cuda")
+    h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)           # BS6
+    np.testing.assert_array_equal(host(gq), orc.gather(ref["rsT"], ref["ciT"], q))
+    g = orc.uniform(ng, 29)
+    dq = torch.zeros(ids.size, dtype=torch.float64, device="cuda")
+    h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)                # BS7
+    np.testing.assert_array_equal(host(dq), orc.scatter(ref["rsT"], ref["ciT"], g,
+                                                        np.zeros(ids.size)))
+
+
+@pytest.mark.parametrize("tcode", [capi.FLOAT, capi.DOUBLE, capi.INT32, capi.INT64])
+@pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
+@pytest.mark.parametrize("k", [1, 3])
+def test_all_types_ops_transposes(cuda, orc, tcode, op, k):
+    rng = np.random.default_rng(1000 * tcode + 10 * op + k)
+    n = 3000
+    keys = rng.integers(1, 700, size=n).astype(np.int64)
+    keys[rng.random(n) < 0.08] = 0            # ignored entries
+    keys[rng.random(n) < 0.3] *= -1           # flagged entries
+    h, ref = make(orc, keys, kind=capi.SIGNED, unique=False)
+    nT, nN = ref["rsT"].size - 1, ref["rsN"].size - 1
+    rsNp = pad(ref["rsN"], nT)
+    dt = NP_TYPES[tcode]
+    v = values(orc, n * k, dt, 5 + op)
+    tv = torch.from_numpy(v).cuda()
+
+    # Gather Trans / NoTrans
+    for trans, (rs, ci, rows) in ((O.Trans, (ref["rsT"], ref["ciT"], nT)),
+                                  (O.NoTrans, (ref["rsN"], ref["ciN"], nN))):
+        gv = torch.zeros(max(rows, 1) * k, dtype=tv.dtype, device="cuda")
+        h.Gather(gv, tv, k, op, trans)
+        np.testing.assert_array_equal(host(gv)[: rows * k], orc.gather(rs, ci, v, k, op),
+                                      err_msg=f"gather trans={trans}")
+    # Scatter NoTrans (T) / Trans (N)
+    for trans, (rs, ci, rows) in ((O.NoTrans, (ref["rsT"], ref["ciT"], nT)),
+                                  (O.Trans, (ref["rsN"], ref["ciN"], nN))):
+        g = values(orc, max(rows, 1) * k, dt, 77)
+        base = values(orc, n * k, dt, 78)
+        dv = torch.from_numpy(base).cuda()
+        h.Scatter(dv, torch.from_numpy(g).cuda(), k, trans)
+        np.testing.assert_array_equal(host(dv), orc.scatter(rs, ci, g[: rows * k], base, k),
+                                      err_msg=f"scatter trans={trans}")
+    # GatherScatter Sym / NoTrans / Trans (op honoured for every transpose)
+    cases = {O.Sym: (ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"]),
+             O.NoTrans: (rsNp, ref["ciN"], ref["rsT"], ref["ciT"]),
+             O.Trans: (ref["rsT"], ref["ciT"], rsNp, ref["ciN"])}
+    for trans, (grs, gci, srs, sci) in cases.items():
+        dv = torch.from_numpy(v).cuda()
+        h.GatherScatter(dv, k, op, trans)
+        np.testing.assert_array_equal(host(dv), orc.gather_scatter(grs, gci, srs, sci, v, k, op),
+                                      err_msg=f"gs trans={trans}")
+
+
+def test_unsigned_handle(cuda, orc):
+    rng = np.random.default_rng(5)
+    n = 2000
+    keys = rng.integers(1, 300, size=n).astype(np.int64)
+    keys[rng.random(n) < 0.5] *= -1
+    h, ref = make(orc, keys, kind=capi.UNSIGNED, unique=False)
+    nN = ref["rsN"].size - 1
+    v = orc.uniform(n, 3)
+    tv = torch.from_numpy(v).cuda()
+    gv = torch.zeros(nN, dtype=torch.float64, device="cuda")
+    h.Gather(gv, tv, 1, O.Add, O.NoTrans)
+    np.testing.assert_array_equal(host(gv), orc.gather(ref["rsN"], ref["ciN"], v))
+    for trans in (O.Sym, O.NoTrans, O.Trans):
+        dv = torch.from_numpy(v).cuda()
+        h.GatherScatter(dv, 1, O.Add, trans)
+        np.testing.assert_array_equal(
+            host(dv), orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], v))
+
+
+def test_negative_zero_and_special_values(cuda, orc):
+    # 0.0 + (-0.0) = +0.0 in the reference's row sums; NaN never wins Max/Min
+    ids = np.array([1, 1, 2, 3, 3, 3], dtype=np.int64)
+    h, ref = make(orc, ids)
+    v = np.array([-0.0, -0.0, -0.0, np.nan, 1.0, -np.inf])
+    for op in (O.Add, O.Max, O.Min, O.Mul):
+        dv = torch.from_numpy(v).cuda()
+        h.GatherScatter(dv, 1, op, O.Sym)
+        want = orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], v, 1, op)
+        got = host(dv)
+        np.testing.assert_array_equal(np.signbit(got), np.signbit(want))
+        np.testing.assert_array_equal(got, want)
+
+
+def test_empty_and_tiny_plans(cuda, orc):
+    h = O.ogs_t()
+    ids = np.zeros(5, dtype=np.int64)
+    h.Setup(5, ids, unique=True)
+    assert h.NgatherGlobal == 0
+    v = torch.ones(5, dtype=torch.float64, device="cuda")
+    h.GatherScatter(v, 1, O.Add, O.Sym)
+    assert host(v).tolist() == [1.0] * 5
+    ids = np.array([7], dtype=np.int64)
+    h.Setup(1, ids, unique=True)
+    v = torch.tensor([-0.0], dtype=torch.float64, device="cuda")
+    h.GatherScatter(v, 1, O.Add, O.Sym)
+    assert not np.signbit(host(v)[0])
+
+
+def test_large_block_boundaries(cuda, orc):
+    """Rows of varied multiplicity (up to the reference's 512 limit) crossing the
+    2048-entry block boundaries."""
+    rng = np.random.default_rng(11)
+    sizes = rng.integers(1, 513, size=300)
+    keys = np.repeat(np.arange(1, sizes.size + 1), sizes).astype(np.int64)
+    rng.shuffle(keys)
+    h, ref = make(orc, keys)
+    v = orc.uniform(keys.size, 8)
+    dv = torch.from_numpy(v).cuda()
+    h.GatherScatter(dv, 1, O.Add, O.Sym)
+    np.testing.assert_array_equal(
+        host(dv), orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], v))
+    assert h.info.maxRowSize == sizes.max()

@@ -1,0 +1,199 @@
+"""BS0-BS5 CUDA kernels against the oracle (GPU).
+
+Copy and axpy are bit-exact; the order-exact reductions are bit-exact with the
+oracle's restatement of the reference's two-stage tree under CUDA-mode
+contraction (fmad); the single-launch reductions are within a stated bound of a
+double-double reference; FP32-storage results are within 1e-6 relative of the
+FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from streamparanumal_gb300 import kernels as K
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [0, 1, 2, 3, 31, 255, 256, 257, 1023, 1024, 1025, 4095, 65537, 1 << 20, (1 << 20) + 3]
+
+
+def dev(x):
+    return torch.from_numpy(x).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("offset", [0, 1])
+def test_bs1_copy_bit_exact(cuda, orc, n, offset):
+    a = orc.uniform(n + offset, 11 + n)
+    da = dev(a)[offset:]
+    db = torch.full((n + offset,), 7.0, dtype=torch.float64, device="cuda")[offset:]
+    K.bs1(n, da, db)
+    np.testing.assert_array_equal(host(db), a[offset:])
+    # f32
+    a32 = a.astype(np.float32)
+    da32 = dev(a32)[offset:]
+    db32 = torch.zeros(n + offset, dtype=torch.float32, device="cuda")[offset:]
+    K.bs1(n, da32, db32)
+    np.testing.assert_array_equal(host(db32), a32[offset:])
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("ab", [(1.0, 1.0), (0.37, -1.9), (-0.731, 0.5)])
+def test_bs2_axpy_bit_exact(cuda, orc, n, ab):
+    alpha, beta = ab
+    x = orc.uniform(n, 100 + n)
+    y = orc.uniform(n, 200 + n)
+    dy = dev(y)
+    K.bs2(n, alpha, dev(x), beta, dy)
+    np.testing.assert_array_equal(host(dy), orc.bs2(alpha, x, beta, y, fmad=1))
+    x32, y32 = x.astype(np.float32), y.astype(np.float32)
+    dy32 = dev(y32)
+    K.bs2(n, alpha, dev(x32), beta, dy32)
+    np.testing.assert_array_equal(host(dy32), orc.bs2(alpha, x32, beta, y32, fmad=1))
+
+
+def test_bs2_misaligned_vectors(cuda, orc):
+    n = 1001
+    x = orc.uniform(n + 1, 5)
+    y = orc.uniform(n + 1, 6)
+    dx, dy = dev(x), dev(y)
+    K.bs2(n, 0.25, dx[1:], -3.0, dy[:n])  # x is 8-byte aligned only
+    np.testing.assert_array_equal(host(dy)[:n], orc.bs2(0.25, x[1:].copy(), -3.0, y[:n].copy()))
+
+
+@pytest.mark.parametrize("n", [1, 5, 256, 257, 65536, 65537, 300000, 1 << 21])
+@pytest.mark.parametrize("bs", [256, 1024])
+def test_bs3_order_exact(cuda, orc, n, bs):
+    a = orc.uniform(n, 300 + n)
+    nb = K.nblocks_for(n, bs)
+    tmp = torch.zeros(bs, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.bs3_1(nb, n, dev(a), tmp, block_size=bs)
+    K.bs3_2(nb, tmp, out, block_size=bs)
+    part, res = orc.bs3(a, bs=bs, nblocks=nb, fmad=1)
+    np.testing.assert_array_equal(host(tmp)[:nb], part)
+    assert host(out)[0] == res
+
+
+@pytest.mark.parametrize("n", [1, 7, 257, 65537, 1 << 20, (1 << 21) + 5])
+@pytest.mark.parametrize("bs", [256, 512])
+def test_bs4_order_exact(cuda, orc, n, bs):
+    a = orc.uniform(n, 400 + n)
+    b = orc.uniform(n, 500 + n)
+    nb = K.nblocks_for(n, bs)
+    tmp = torch.zeros(bs, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.bs4_1(nb, n, dev(a), dev(b), tmp, block_size=bs)
+    K.bs4_2(nb, tmp, out, block_size=bs)
+    part, res = orc.bs4(a, b, bs=bs, nblocks=nb, fmad=1)
+    np.testing.assert_array_equal(host(tmp)[:nb], part)
+    assert host(out)[0] == res
+    # and the dot is within 1e-14 relative... of the exact value only when no
+    # cancellation; the fixed order is what makes it reproducible
+    exact = orc.dot_dd(a, b)
+    assert abs(res - exact) <= 1e-12 * max(1.0, np.abs(a * b).sum())
+
+
+@pytest.mark.parametrize("n", [1, 1023, 1024, 1025, 1 << 20, (1 << 21) + 9])
+@pytest.mark.parametrize("bs", [1024, 256])
+def test_bs5_order_exact(cuda, orc, n, bs):
+    Ap = orc.uniform(n, 600 + n)
+    r = orc.uniform(n, 700 + n)
+    alpha = -0.6180339887
+    nb = K.nblocks_for(n, bs)
+    dr = dev(r)
+    tmp = torch.zeros(bs, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.bs5_1(nb, n, dev(Ap), alpha, dr, tmp, block_size=bs)
+    K.bs5_2(nb, tmp, out, block_size=bs)
+    r_ref, part, res = orc.bs5(Ap, alpha, r, bs=bs, nblocks=nb, fmad=1)
+    np.testing.assert_array_equal(host(dr), r_ref)
+    np.testing.assert_array_equal(host(tmp)[:nb], part)
+    assert host(out)[0] == res
+
+
+def test_reference_driver_nblock_rule():
+    # Nblock = min(ceil(N/bs), bs) (BS/BS3/src/bs3Run.cpp:80-81)
+    assert K.nblocks_for(1, 256) == 1
+    assert K.nblocks_for(257, 256) == 2
+    assert K.nblocks_for(1 << 28, 256) == 256
+    assert K.nblocks_for(1 << 28, 1024) == 1024
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 1000, 65537, 1 << 22])
+def test_fast_reductions_fp64(cuda, orc, n):
+    a = orc.uniform(n, 800 + n)
+    b = orc.uniform(n, 900 + n)
+    sc = K.ReduceScratch()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.dot(dev(a), dev(b), out, sc)
+    exact = orc.dot_dd(a, b)
+    # fixed-grid pairwise-like order: error <= n * eps * sum|ab| (loose bound)
+    bound = 4 * max(n, 1) * 2.2e-16 * float(np.abs(a * b).sum()) + 1e-300
+    assert abs(host(out)[0] - exact) <= bound
+    K.norm2(dev(a), out, sc)
+    exact = orc.dot_dd(a, a)
+    assert abs(host(out)[0] - exact) <= 1e-14 * max(exact, 1e-300) * 8
+    # scratch is left zeroed: a second call gives the same bits
+    first = host(out)[0]
+    K.norm2(dev(a), out, sc)
+    assert host(out)[0] == first
+
+
+@pytest.mark.parametrize("n", [1, 5, 1000, 65537, 1 << 22])
+def test_fast_reductions_fp32_storage(cuda, orc, n):
+    a = orc.uniform(n, 1000 + n)
+    b = orc.uniform(n, 1100 + n)
+    a32, b32 = a.astype(np.float32), b.astype(np.float32)
+    sc = K.ReduceScratch()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.norm2(dev(a32), out, sc)
+    ref = orc.dot_dd(a32, a32)  # FP64 oracle on the stored FP32 values
+    assert abs(host(out)[0] - ref) <= 1e-6 * ref
+    K.dot(dev(a32), dev(b32), out, sc)
+    ref = orc.dot_dd(a32, b32)
+    scale = float(np.abs(a32.astype(np.float64) * b32).sum())
+    assert abs(host(out)[0] - ref) <= 1e-6 * max(abs(ref), 1e-3 * scale)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 1001, 65536, (1 << 21) + 1])
+def test_cg_update_fp64(cuda, orc, n):
+    x, r, p, Ap = (orc.uniform(n, s + n) for s in (1, 2, 3, 4))
+    alpha = 0.318309886
+    dx, dr = dev(x), dev(r)
+    sc = K.ReduceScratch()
+    rr = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.cg_update(alpha, dev(p), dev(Ap), dx, dr, rr, sc)
+    xr, rref, rrref = orc.cg_update(alpha, p, Ap, x, r)
+    np.testing.assert_array_equal(host(dx), xr)
+    np.testing.assert_array_equal(host(dr), rref)
+    assert abs(host(rr)[0] - rrref) <= 1e-14 * rrref * 8
+
+
+@pytest.mark.parametrize("n", [1, 3, 4, 1001, 65536, (1 << 21) + 3])
+def test_cg_update_fp32_storage(cuda, orc, n):
+    x, r, p, Ap = (orc.uniform(n, 10 * s + n).astype(np.float32) for s in (1, 2, 3, 4))
+    alpha = 0.318309886
+    dx, dr = dev(x), dev(r)
+    sc = K.ReduceScratch()
+    rr = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.cg_update(alpha, dev(p), dev(Ap), dx, dr, rr, sc)
+    xr, rref, rrref = orc.cg_update(np.float32(alpha), p, Ap, x, r)
+    np.testing.assert_array_equal(host(dx), xr)
+    np.testing.assert_array_equal(host(dr), rref)
+    assert abs(host(rr)[0] - rrref) <= 1e-6 * rrref
+
+
+def test_bs0_and_graph(cuda):
+    a = torch.zeros(1, dtype=torch.float64, device="cuda")
+    b = torch.full((1,), 5.0, dtype=torch.float64, device="cuda")
+    K.bs0(1, a, b)
+    g = K.Bs0Graph(100, 1, a, b)
+    g.launch()
+    assert host(b)[0] == 5.0  # n != 0: no store
+    K.bs0(0, a, b)
+    assert host(b)[0] == 0.0  # n == 0: the guarded store happens
