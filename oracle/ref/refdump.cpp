@@ -56,6 +56,8 @@ class refSettings_t : public settings_t {
   refSettings_t(int argc, char** argv, comm_t c) : settings_t(c) {
     platformAddSettings(*this);
     meshAddSettings(*this);
+    newSetting("-v", "--verbose", "VERBOSE", "FALSE", "Enable verbose output",
+               {"TRUE", "FALSE"});
     parseSettings(argc, argv);
   }
 };

@@ -43,10 +43,12 @@ class json {
     if (slash == std::string::npos) return obj[key];
     return obj[key.substr(0, slash)][key.substr(slash + 1)];
   }
+  json& operator[](const char* key) { return (*this)[std::string(key)]; }
   json& operator=(const std::string& s) { kind = string_; str = s; return *this; }
   json& operator=(const char* s) { kind = string_; str = s; return *this; }
   json& operator=(bool v) { kind = bool_; b = v; return *this; }
   json& operator=(int v) { kind = number_; num = v; str = std::to_string(v); return *this; }
+  json& operator=(long v) { kind = number_; num = (double)v; str = std::to_string(v); return *this; }
   json& operator=(long long v) { kind = number_; num = (double)v; str = std::to_string(v); return *this; }
   json& operator=(float v) { kind = number_; num = v; str = std::to_string(v); return *this; }
   json& operator=(double v) { kind = number_; num = v; str = std::to_string(v); return *this; }
@@ -54,7 +56,6 @@ class json {
   json& asObject() { if (kind == none_) kind = object_; return *this; }
   json& asArray() { if (kind == none_) kind = array_; return *this; }
   bool has(const std::string& key) const { return obj.count(key) != 0; }
-  operator bool() const { return b; }
   std::string toString() const { return str; }
 };
 
@@ -119,6 +120,12 @@ class memory {
   void free() {
     buf = nullptr;
     offset_ = size_ = 0;
+  }
+  void swap(memory& m) {
+    std::swap(buf, m.buf);
+    std::swap(offset_, m.offset_);
+    std::swap(size_, m.size_);
+    std::swap(elem_, m.elem_);
   }
 };
 
