@@ -57,6 +57,13 @@ int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch
  * since the last reset (used by harnesses to count launches in a timed region). */
 int64_t     sp_launch_count(void);
 void        sp_launch_count_reset(void);
+/* Tuning knobs selecting among compiled kernel variants (process-wide; the
+ * autotuner's surface).  Keys: "reduce.prefetch_chunks" (0..64, default 8): L2
+ * bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
+ * (256..2048, default 2048): non-zeros per row block of plans created afterwards.
+ * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
+sp_status   sp_tune_set(const char* key, int64_t value);
+sp_status   sp_tune_get(const char* key, int64_t* value);
 
 /* ---------------------------------------------------------------- BS0
  * Empty 1x1 launch.  Replaces the `bs0` kernel (BS/BS0/okl/bs0.okl:27-39) launched

@@ -59,6 +59,8 @@ SIGNATURES = {
     "sp_version": (c_int32, []),
     "sp_launch_count": (c_int64, []),
     "sp_launch_count_reset": (None, []),
+    "sp_tune_set": (c_int32, [ctypes.c_char_p, c_int64]),
+    "sp_tune_get": (c_int32, [ctypes.c_char_p, _I64P]),
     "sp_bs0": (c_int32, [c_int32, _P, _P, _P]),
     "sp_bs0_graph_create": (c_int32, [c_int32, c_int32, _P, _P, _P, POINTER(c_void_p)]),
     "sp_graph_launch": (c_int32, [_P, _P]),

@@ -37,6 +37,15 @@ inline cudaStream_t as_cuda(sp_stream_t s) { return reinterpret_cast<cudaStream_
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// ---------------------------------------------------------------- tuning knobs
+// Runtime-selectable launch parameters (the autotuner's surface, sp_tune_set/get).
+enum TuneKey : int {
+  kTuneReducePrefetch = 0,  // order-exact reductions: L2 bulk-prefetch distance in chunks (0 = off)
+  kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
+  kTuneCount
+};
+int64_t tune(TuneKey k);
+
 // ---------------------------------------------------------------- scratch layout
 // Layout of the caller-provided scratch of the single-launch reductions:
 //   [0, 8)                 : unsigned int ticket counter (+4 bytes pad)

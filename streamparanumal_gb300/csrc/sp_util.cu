@@ -1,5 +1,7 @@
 // Library-wide utilities: error strings, launch counter, BS0 graph objects.
+#include <atomic>
 #include <cstdarg>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -22,6 +24,18 @@ sp_status fail(sp_status s, const char* fmt, ...) {
 
 void clear_error() { t_last_error.clear(); }
 void count_launch(int64_t n) { t_launches += n; }
+
+struct TuneEntry {
+  const char* name;
+  int64_t lo, hi;
+  std::atomic<int64_t> value;
+};
+static TuneEntry g_tune[kTuneCount] = {
+    {"reduce.prefetch_chunks", 0, 64, {8}},
+    {"ogs.block_nnz", 256, 2048, {2048}},
+};
+
+int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }
 
 int sm_count() {
   static std::mutex mu;
@@ -63,6 +77,29 @@ const char* sp_status_string(sp_status s) {
 int32_t sp_version(void) { return 100; }  // 0.1.0
 
 int64_t sp_launch_count(void) { return sp::t_launches; }
+
+sp_status sp_tune_set(const char* key, int64_t value) {
+  if (!key) return sp::fail(SP_ERR_INVALID_ARG, "sp_tune_set: null key");
+  for (auto& e : sp::g_tune)
+    if (std::strcmp(e.name, key) == 0) {
+      if (value < e.lo || value > e.hi)
+        return sp::fail(SP_ERR_INVALID_ARG, "sp_tune_set: %s=%lld outside [%lld, %lld]", key,
+                        (long long)value, (long long)e.lo, (long long)e.hi);
+      e.value.store(value, std::memory_order_relaxed);
+      return SP_SUCCESS;
+    }
+  return sp::fail(SP_ERR_INVALID_ARG, "sp_tune_set: unknown key '%s'", key);
+}
+
+sp_status sp_tune_get(const char* key, int64_t* value) {
+  if (!key || !value) return sp::fail(SP_ERR_INVALID_ARG, "sp_tune_get: null argument");
+  for (auto& e : sp::g_tune)
+    if (std::strcmp(e.name, key) == 0) {
+      *value = e.value.load(std::memory_order_relaxed);
+      return SP_SUCCESS;
+    }
+  return sp::fail(SP_ERR_INVALID_ARG, "sp_tune_get: unknown key '%s'", key);
+}
 void sp_launch_count_reset(void) { sp::t_launches = 0; }
 
 }  // extern "C"

@@ -196,15 +196,43 @@ __device__ __forceinline__ double tree_reduce(double v, double* s) {
 }
 
 // Lane t of logical block b visits t + b*BS + j*BS*nblocks for j = 0, 1, ...
-// (bs3.okl:36-41).  U loads are issued ahead of the in-order accumulation.
+// (bs3.okl:36-41).  For a fixed j the block's lanes read one contiguous chunk of
+// BS values, so each CTA streams through its chunks j = 0, 1, 2, ...  Two things
+// keep enough bytes in flight with only nblocks*BS lanes:
+//   * U chunks' loads are issued ahead of the in-order accumulation;
+//   * with pd > 0, lanes of warp 0 issue cp.async.bulk.prefetch.L2 for the chunks
+//     pd ahead, so the lanes' loads hit L2 (fire-and-forget: nothing waits on it).
+
+// Bulk L2 prefetch of `bytes` (multiple of 16) from a 16-byte aligned address.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Prefetch chunk j (BS doubles at base + j*stride) of x, clipped to n.
+template <int BS>
+__device__ __forceinline__ void prefetch_chunk(const double* x, int64_t base, int64_t stride,
+                                               int64_t j, int64_t n) {
+  const int64_t start = base + j * stride;
+  if (start >= n) return;
+  const int64_t cnt = (n - start < BS) ? (n - start) : BS;
+  const uint32_t bytes = (uint32_t)(cnt * 8) & ~15u;
+  if (bytes) prefetch_l2(x + start, bytes);
+}
+
 template <int BS, int U>
 __global__ void __launch_bounds__(BS)
-k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict__ partial) {
+k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict__ partial,
+        int pd) {
   __shared__ double s[BS];
+  const int t = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * BS;
   const int64_t stride = (int64_t)BS * nblocks;
-  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  const bool pf = pd > 0 && ((reinterpret_cast<uintptr_t>(a) & 15u) == 0);
+  if (pf && t < pd) prefetch_chunk<BS>(a, base, stride, t, n);
+  int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride) {
+  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+    if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
     double v[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) v[u] = __ldcs(a + id + u * stride);
@@ -216,18 +244,26 @@ k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict
     acc = fma(v, v, acc);
   }
   const double r = tree_reduce<BS>(acc, s);
-  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+  if (t == 0) partial[blockIdx.x] = r;
 }
 
 template <int BS, int U>
 __global__ void __launch_bounds__(BS)
 k_bs4_1(int nblocks, int64_t n, const double* __restrict__ a, const double* __restrict__ b,
-        double* __restrict__ partial) {
+        double* __restrict__ partial, int pd) {
   __shared__ double s[BS];
+  const int t = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * BS;
   const int64_t stride = (int64_t)BS * nblocks;
-  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  const bool pf = pd > 0 && (((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) &
+                              15u) == 0);
+  if (pf && t < pd) prefetch_chunk<BS>(a, base, stride, t, n);
+  if (pf && t >= 32 && t < 32 + pd) prefetch_chunk<BS>(b, base, stride, t - 32, n);
+  int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride) {
+  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+    if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
+    if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(b, base, stride, j + pd + t - 32, n);
     double va[U], vb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -239,18 +275,26 @@ k_bs4_1(int nblocks, int64_t n, const double* __restrict__ a, const double* __re
   }
   for (; id < n; id += stride) acc = fma(__ldcs(a + id), __ldcs(b + id), acc);
   const double r = tree_reduce<BS>(acc, s);
-  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+  if (t == 0) partial[blockIdx.x] = r;
 }
 
 template <int BS, int U>
 __global__ void __launch_bounds__(BS)
 k_bs5_1(int nblocks, int64_t n, const double* __restrict__ Ap, double alpha, double* __restrict__ r,
-        double* __restrict__ partial) {
+        double* __restrict__ partial, int pd) {
   __shared__ double s[BS];
+  const int t = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * BS;
   const int64_t stride = (int64_t)BS * nblocks;
-  int64_t id = threadIdx.x + (int64_t)blockIdx.x * BS;
+  const bool pf = pd > 0 && (((reinterpret_cast<uintptr_t>(Ap) | reinterpret_cast<uintptr_t>(r)) &
+                              15u) == 0);
+  if (pf && t < pd) prefetch_chunk<BS>(r, base, stride, t, n);
+  if (pf && t >= 32 && t < 32 + pd) prefetch_chunk<BS>(Ap, base, stride, t - 32, n);
+  int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride) {
+  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+    if (pf && t < U) prefetch_chunk<BS>(r, base, stride, j + pd + t, n);
+    if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(Ap, base, stride, j + pd + t - 32, n);
     double vr[U], va[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -270,7 +314,7 @@ k_bs5_1(int nblocks, int64_t n, const double* __restrict__ Ap, double alpha, dou
     acc = fma(rr, rr, acc);
   }
   const double res = tree_reduce<BS>(acc, s);
-  if (threadIdx.x == 0) partial[blockIdx.x] = res;
+  if (t == 0) partial[blockIdx.x] = res;
 }
 
 // Stage 2 (bs3.okl:66-102): lane t holds 0.0 + partial[t] (t < nblocks, each lane
@@ -614,9 +658,10 @@ sp_status sp_bs3_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, 
   if (st) return st;
   if (!partial || (n > 0 && !a)) return fail(SP_ERR_INVALID_ARG, "sp_bs3_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  if (bs == 256) k_bs3_1<256, 16><<<nblocks, 256, 0, s>>>(nblocks, n, a, partial);
-  else if (bs == 512) k_bs3_1<512, 8><<<nblocks, 512, 0, s>>>(nblocks, n, a, partial);
-  else k_bs3_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, partial);
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (bs == 256) k_bs3_1<256, 16><<<nblocks, 256, 0, s>>>(nblocks, n, a, partial, pd);
+  else if (bs == 512) k_bs3_1<512, 8><<<nblocks, 512, 0, s>>>(nblocks, n, a, partial, pd);
+  else k_bs3_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, partial, pd);
   return check_launch("sp_bs3_1_f64");
 }
 
@@ -627,9 +672,10 @@ sp_status sp_bs4_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, 
   if (!partial || (n > 0 && (!a || !b)))
     return fail(SP_ERR_INVALID_ARG, "sp_bs4_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial);
-  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial);
-  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial);
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial, pd);
+  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial, pd);
+  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial, pd);
   return check_launch("sp_bs4_1_f64");
 }
 
@@ -640,9 +686,10 @@ sp_status sp_bs5_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* Ap,
   if (!partial || (n > 0 && (!Ap || !r)))
     return fail(SP_ERR_INVALID_ARG, "sp_bs5_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  if (bs == 256) k_bs5_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
-  else if (bs == 512) k_bs5_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
-  else k_bs5_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, Ap, alpha, r, partial);
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (bs == 256) k_bs5_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
+  else if (bs == 512) k_bs5_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
+  else k_bs5_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
   return check_launch("sp_bs5_1_f64");
 }
 
