@@ -117,6 +117,23 @@ sp_status sp_bs5_1_f64(int32_t block_size, int32_t nblocks, int64_t n, const dou
 sp_status sp_reduce_finish_f64(int32_t block_size, int32_t nblocks, const double* partial,
                                double* out, sp_stream_t stream);
 
+/* ---------------------------------------------------------------- allocation-free dot
+ * No counterpart in the reference.  The BS4 dot (bs4_1 then bs4_2, bit-identical to
+ * sp_bs4_1_f64 + sp_reduce_finish_f64) for callers that cannot allocate device
+ * memory -- their device memory belongs to another allocator or a fixed pool, or
+ * they cannot afford cudaMalloc's device-wide synchronisation -- and therefore
+ * cannot supply the partial-sum buffer.  The partials live in a static 1024-double
+ * array inside the library (8 KiB held on every GPU that loads it, until exit):
+ *  - nblocks must not exceed 1024 (larger values fail with SP_ERR_SIZE);
+ *  - the first call on a device looks up the array's device address (set-up);
+ *    make that first call before any stream capture;
+ *  - every call shares the one array, so calls that overlap on the GPU (other
+ *    streams, other host threads) race; serialise them on one stream;
+ *  - nothing in the array has to start at zero: each call writes the partials it
+ *    reads.  Allocates nothing. */
+sp_status sp_bs4_dot_f64_noalloc(int32_t block_size, int32_t nblocks, int64_t n, const double* a,
+                                 const double* b, double* out, sp_stream_t stream);
+
 /* ---------------------------------------------------------------- fast reductions
  * Single-launch reductions over a fixed grid (deterministic for a given n, but
  * not the reference's summation order).  `scratch` must hold

@@ -73,6 +73,7 @@ SIGNATURES = {
     "sp_bs4_1_f64": (c_int32, [c_int32, c_int32, c_int64, _P, _P, _P, _P]),
     "sp_bs5_1_f64": (c_int32, [c_int32, c_int32, c_int64, _P, c_double, _P, _P, _P]),
     "sp_reduce_finish_f64": (c_int32, [c_int32, c_int32, _P, _P, _P]),
+    "sp_bs4_dot_f64_noalloc": (c_int32, [c_int32, c_int32, c_int64, _P, _P, _P, _P]),
     "sp_reduce_scratch_bytes": (c_size_t, []),
     "sp_norm2_f64": (c_int32, [c_int64, _P, _P, _P, _P]),
     "sp_dot_f64": (c_int32, [c_int64, _P, _P, _P, _P, _P]),

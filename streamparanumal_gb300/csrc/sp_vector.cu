@@ -10,6 +10,7 @@
 //   bs5:  r + alpha*Ap       -> fma(alpha, Ap, r);  acc += r*r -> fma(r, r, acc)
 #include <cstdint>
 #include <initializer_list>
+#include <mutex>
 
 #include "sp_internal.h"
 
@@ -832,6 +833,77 @@ sp_status sp_graph_destroy(sp_graph* g) {
   if (g->graph) cudaGraphDestroy(g->graph);
   delete g;
   return SP_SUCCESS;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free BS4 dot
+//
+// For callers that cannot allocate device memory themselves -- e.g. a solver whose
+// device memory all belongs to another allocator or a fixed pool, or code that must
+// not pay cudaMalloc's device-wide synchronisation inside its loop -- and so cannot
+// provide the partial-sum buffer that sp_bs4_1_f64 needs.  The partial sums live
+// in a static device array of the library instead: every GPU that loads the
+// library holds these kNoAllocMaxBlocks doubles (8 KiB) until the process exits.
+
+namespace sp {
+
+constexpr int kNoAllocMaxBlocks = 1024;
+static __device__ __align__(256) double g_noalloc_partial[kNoAllocMaxBlocks];
+
+// Device address of g_noalloc_partial, looked up once per device (with that device
+// current) on the first call there.
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+static sp_status noalloc_partials(double** out) {
+  int dev = 0;
+  SP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(SP_ERR_UNSUPPORTED, "sp_bs4_dot_f64_noalloc: device %d beyond %d", dev,
+                kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
+    if (e != cudaSuccess || !p)
+      return fail(SP_ERR_CUDA, "sp_bs4_dot_f64_noalloc: cudaGetSymbolAddress failed: %s",
+                  cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return SP_SUCCESS;
+}
+
+}  // namespace sp
+
+extern "C" {
+
+sp_status sp_bs4_dot_f64_noalloc(int32_t bs, int32_t nblocks, int64_t n, const double* a,
+                                 const double* b, double* out, sp_stream_t stream) {
+  if (nblocks > kNoAllocMaxBlocks)
+    return fail(SP_ERR_SIZE,
+                "sp_bs4_dot_f64_noalloc: nblocks %d exceeds the static partial-sum capacity %d",
+                nblocks, kNoAllocMaxBlocks);
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs4_dot_f64_noalloc");
+  if (st) return st;
+  if (!out || (n > 0 && (!a || !b)))
+    return fail(SP_ERR_INVALID_ARG, "sp_bs4_dot_f64_noalloc: null pointer");
+  double* partial = nullptr;
+  if ((st = noalloc_partials(&partial))) return st;
+  // stage 1 writes partial[0, nblocks) in full before stage 2 reads it, so nothing
+  // in the shared array has to start at zero
+  cudaStream_t s = as_cuda(stream);
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial, pd);
+  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial, pd);
+  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial, pd);
+  if ((st = check_launch("sp_bs4_dot_f64_noalloc"))) return st;
+  if (bs == 256) k_finish<256><<<1, 256, 0, s>>>(nblocks, partial, out);
+  else if (bs == 512) k_finish<512><<<1, 512, 0, s>>>(nblocks, partial, out);
+  else k_finish<1024><<<1, 1024, 0, s>>>(nblocks, partial, out);
+  return check_launch("sp_bs4_dot_f64_noalloc");
 }
 
 }  // extern "C"
