@@ -58,9 +58,12 @@ int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch
 int64_t     sp_launch_count(void);
 void        sp_launch_count_reset(void);
 /* Tuning knobs selecting among compiled kernel variants (process-wide; the
- * autotuner's surface).  Keys: "reduce.prefetch_chunks" (0..64, default 8): L2
+ * autotuner's surface).  Keys: "reduce.prefetch_chunks" (0..64, default 4): L2
  * bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
- * (256..2048, default 2048): non-zeros per row block of plans created afterwards.
+ * (256..2048, default 2048): non-zeros per row block of plans created afterwards;
+ * "ogs.kernel" (0 block kernels, 1 warp-chunk kernels; default 1); "ogs.order"
+ * (0 row order, 1 breadth-first over 4 KiB pages; default 1) for the warp chunks of
+ * plans created afterwards.
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);
@@ -183,6 +186,10 @@ typedef struct {
   int32_t NrowBlocksN;
   int32_t maxRowSize; /* largest group                                          */
   int64_t NgatherGlobal;
+  int32_t NchunksT;   /* warp chunks of the T / N operators (0: block kernels only) */
+  int32_t NchunksN;
+  int32_t chunkOrder; /* 0 row order, 1 breadth-first over 4 KiB pages             */
+  int32_t reserved;
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

@@ -45,7 +45,8 @@ class SpError(RuntimeError):
 class OgsInfo(ctypes.Structure):
     _fields_ = [("N", c_int32), ("NrowsT", c_int32), ("NrowsN", c_int32), ("nnzT", c_int32),
                 ("nnzN", c_int32), ("NrowBlocksT", c_int32), ("NrowBlocksN", c_int32),
-                ("maxRowSize", c_int32), ("NgatherGlobal", c_int64)]
+                ("maxRowSize", c_int32), ("NgatherGlobal", c_int64), ("NchunksT", c_int32),
+                ("NchunksN", c_int32), ("chunkOrder", c_int32), ("reserved", c_int32)]
 
 
 _P = c_void_p
@@ -142,6 +143,16 @@ def call(name: str, *args):
 def status(name: str, *args) -> int:
     """Call an entry point and return its status without raising."""
     return getattr(load(), name)(*args)
+
+
+def tune_set(key: str, value: int) -> None:
+    call("sp_tune_set", key.encode(), int(value))
+
+
+def tune_get(key: str) -> int:
+    v = c_int64()
+    call("sp_tune_get", key.encode(), ctypes.byref(v))
+    return v.value
 
 
 def i32p(arr):

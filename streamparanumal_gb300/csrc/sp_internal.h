@@ -42,6 +42,8 @@ int sm_count();
 enum TuneKey : int {
   kTuneReducePrefetch = 0,  // order-exact reductions: L2 bulk-prefetch distance in chunks (0 = off)
   kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
+  kTuneOgsKernel,           // ogs: 0 = block kernels, 1 = warp-chunk kernels (k == 1 only)
+  kTuneOgsOrder,            // ogs plan: warp-chunk order, 0 = rows, 1 = breadth-first pages
   kTuneCount
 };
 int64_t tune(TuneKey k);

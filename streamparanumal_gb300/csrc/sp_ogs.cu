@@ -194,13 +194,140 @@ k_ogs_scatter(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs
   }
 }
 
+// ------------------------------------------------------------------ warp-chunk kernels (k == 1)
+//
+// One warp per chunk of at most 256 non-zeros (a contiguous row range, see
+// sp_ogs_order.cpp).  Each lane loads 8 column ids and issues its 8 gathers before
+// using any of them; the values and the chunk's row starts go to the warp's own
+// slice of shared memory; one lane per row combines in CSR order; results go back
+// coalesced.  Only __syncwarp separates the phases, so warps advance
+// independently and the SM keeps many chunks' loads in flight.
+
+template <typename T>
+struct WarpSmem {
+  T val[kWarpsPerCta][kWarpChunkNnz];
+  int32_t rs[kWarpsPerCta][kWarpChunkNnz + 8];
+};
+
+template <typename T>
+__device__ __forceinline__ void warp_stage(const int32_t* __restrict__ ids, int32_t g0, int32_t gn,
+                                           const T* v, T* sv, int lane,
+                                           int32_t (&col)[kOgsPerLane]) {
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u) {
+    const int i = lane + 32 * u;
+    col[u] = (i < gn) ? __ldg(ids + g0 + i) : 0;
+  }
+  T val[kOgsPerLane];
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < gn) val[u] = v[col[u]];
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kOgsThreads, 6)
+k_ogsw_gs_sym(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, T* __restrict__ v) {
+  __shared__ WarpSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  const int2 ch = __ldg(chunks + c);
+  const int32_t nr = ch.y - ch.x;
+  const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
+  T* sv = sm.val[w];
+  int32_t* srs = sm.rs[w];
+  for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + ch.x + r) - g0;
+  int32_t col[kOgsPerLane];
+  warp_stage<T>(ids, g0, gn, v, sv, lane, col);
+  __syncwarp();
+  for (int32_t r = lane; r < nr; r += 32) {
+    const int32_t a = srs[r], b = srs[r + 1];
+    T acc = Op<T, OP>::init();
+    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+    for (int32_t i = a; i < b; ++i) sv[i] = acc;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogsw_gather(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv) {
+  __shared__ WarpSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  const int2 ch = __ldg(chunks + c);
+  const int32_t nr = ch.y - ch.x;
+  const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
+  T* sv = sm.val[w];
+  int32_t* srs = sm.rs[w];
+  for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + ch.x + r) - g0;
+  int32_t col[kOgsPerLane];
+  warp_stage<T>(ids, g0, gn, v, sv, lane, col);
+  __syncwarp();
+  for (int32_t r = lane; r < nr; r += 32) {
+    const int32_t a = srs[r], b = srs[r + 1];
+    T acc = Op<T, OP>::init();
+    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+    gv[ch.x + r] = acc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogsw_scatter(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v) {
+  __shared__ WarpSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  const int2 ch = __ldg(chunks + c);
+  const int32_t nr = ch.y - ch.x;
+  const int32_t s0 = __ldg(rs + ch.x), sn = __ldg(rs + ch.y) - s0;
+  T* sv = sm.val[w];
+  int32_t col[kOgsPerLane];
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u) {
+    const int i = lane + 32 * u;
+    col[u] = (i < sn) ? __ldg(ids + s0 + i) : 0;
+  }
+  for (int32_t r = lane; r < nr; r += 32) {
+    const T x = gv[ch.x + r];
+    const int32_t a = __ldg(rs + ch.x + r) - s0, b = __ldg(rs + ch.x + r + 1) - s0;
+    for (int32_t i = a; i < b; ++i) sv[i] = x;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < sn) v[col[u]] = sv[lane + 32 * u];
+}
+
+static inline unsigned warp_grid(int32_t nchunks) {
+  return (unsigned)((nchunks + kWarpsPerCta - 1) / kWarpsPerCta);
+}
+
+static inline bool use_warp(const sp_ogs_plan* p, int K, int32_t nchunks) {
+  return K == 1 && nchunks > 0 && tune(kTuneOgsKernel) == 1;
+}
+
 // ------------------------------------------------------------------ dispatch
 
 template <typename T, int OP>
 static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
-  if (trans == SP_SYM || p->n_is_t) {
+  if ((trans == SP_SYM || p->n_is_t) && use_warp(p, K, p->nchunksT)) {
+    k_ogsw_gs_sym<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT, v);
+  } else if (trans == SP_SYM || p->n_is_t) {
     k_ogs_gs_sym<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
                                                      v, K);
   } else if (trans == SP_NOTRANS) {  // gather N, scatter T
@@ -216,7 +343,15 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
 template <typename T, int OP>
 static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
                           cudaStream_t s) {
-  if (trans == SP_NOTRANS) {
+  if (trans == SP_NOTRANS && use_warp(p, K, p->nchunksN)) {
+    k_ogsw_gather<T, OP><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int2*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        p->d_colIdsN, v, gv);
+  } else if (trans != SP_NOTRANS && use_warp(p, K, p->nchunksT)) {
+    k_ogsw_gather<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        v, gv);
+  } else if (trans == SP_NOTRANS) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_gather<T, OP><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
         p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, v, gv, K);
@@ -230,7 +365,15 @@ static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv
 template <typename T>
 static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, const T* gv,
                            cudaStream_t s) {
-  if (trans == SP_TRANS) {
+  if (trans == SP_TRANS && use_warp(p, K, p->nchunksN)) {
+    k_ogsw_scatter<T><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int2*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        p->d_colIdsN, gv, v);
+  } else if (trans != SP_TRANS && use_warp(p, K, p->nchunksT)) {
+    k_ogsw_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        gv, v);
+  } else if (trans == SP_TRANS) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_scatter<T><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
         p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, gv, v, K);
@@ -277,12 +420,13 @@ static sp_status check_common(const sp_ogs_plan* p, sp_type type, int32_t op, in
 // ------------------------------------------------------------------ plan construction
 
 bool partition_rows(int32_t nrows, const int32_t* rs, std::vector<int32_t>& blocks) {
+  const int32_t cap = (int32_t)tune(kTuneOgsBlockNnz);
   blocks.clear();
   blocks.push_back(0);
   int32_t b0 = 0;
   for (int32_t row = 0; row < nrows; ++row) {
-    if (rs[row + 1] - rs[row] > kOgsBlockNnz) return false;
-    if (rs[row + 1] - rs[b0] > kOgsBlockNnz || row - b0 >= kOgsBlockNnz) {
+    if (rs[row + 1] - rs[row] > cap) return false;
+    if (rs[row + 1] - rs[b0] > cap || row - b0 >= cap) {
       blocks.push_back(row);
       b0 = row;
     }
@@ -320,6 +464,11 @@ static void free_plan_device(sp_ogs_plan* p) {
     if (p->d_colIdsN) cudaFree(p->d_colIdsN);
   }
   if (p->own_blocks_n && p->d_blocksN) cudaFree(p->d_blocksN);
+  if (p->own_chunks_n && p->d_chunksN) cudaFree(p->d_chunksN);
+  if (p->d_chunksT) cudaFree(p->d_chunksT);
+  p->d_chunksT = p->d_chunksN = nullptr;
+  p->nchunksT = p->nchunksN = 0;
+  p->own_chunks_n = false;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
   for (int32_t* q : ptrs)
     if (q) cudaFree(q);
@@ -409,6 +558,23 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     p->own_blocks_n = true;
     if ((st = upload(blocksN, &p->d_blocksN, s))) return st;
   }
+  // warp chunks (only when every row fits one chunk)
+  p->chunk_order = (int32_t)tune(kTuneOgsOrder);
+  std::vector<int32_t> chunksT, chunksN;
+  if (build_chunks(p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), p->N, p->chunk_order,
+                   chunksT) &&
+      build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, p->chunk_order,
+                   chunksN)) {
+    p->nchunksT = (int32_t)(chunksT.size() / 2);
+    p->nchunksN = (int32_t)(chunksN.size() / 2);
+    if ((st = upload(chunksT, &p->d_chunksT, s))) return st;
+    if (chunksN == chunksT) {
+      p->d_chunksN = p->d_chunksT;
+    } else {
+      p->own_chunks_n = true;
+      if ((st = upload(chunksN, &p->d_chunksN, s))) return st;
+    }
+  }
   SP_CUDA_TRY(cudaStreamSynchronize(s));
   return SP_SUCCESS;
 }
@@ -488,6 +654,9 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->NrowBlocksN = p->NrowBlocksN;
   info->maxRowSize = p->maxRowSize;
   info->NgatherGlobal = p->NrowsN;
+  info->NchunksT = p->nchunksT;
+  info->NchunksN = p->nchunksN;
+  info->chunkOrder = p->chunk_order;
   return SP_SUCCESS;
 }
 

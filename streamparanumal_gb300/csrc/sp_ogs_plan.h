@@ -14,6 +14,9 @@ constexpr int kOgsPerLane  = 8;
 constexpr int kOgsBlockNnz = kOgsThreads * kOgsPerLane;   // 2048
 // The reference refuses groups larger than this (libs/ogs/ogsOperator.cpp:535).
 constexpr int kOgsMaxRowSize = 512;
+// Warp chunks: at most 256 non-zeros (8 per lane) and 256 rows, one warp each.
+constexpr int kWarpChunkNnz = 256;
+constexpr int kWarpsPerCta = 8;
 
 struct OgsOperatorDev {
   int32_t nrows = 0;       // rows covered by `blocks`
@@ -26,6 +29,12 @@ struct OgsOperatorDev {
 // Greedy partition of rows into blocks of at most kOgsBlockNnz non-zeros and at
 // most kOgsBlockNnz rows.  Returns false when one row alone is too large.
 bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t>& blocks);
+
+// Cuts rows [0, nrows) into warp chunks, stored as (first row, end row) pairs in the
+// order they are scheduled: 0 = row order, 1 = breadth-first over 4 KiB pages of
+// local data.  Returns false when a row holds more than kWarpChunkNnz entries.
+bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
+                  int order, std::vector<int32_t>& chunks);
 
 }  // namespace sp
 
@@ -47,6 +56,13 @@ struct sp_ogs_plan {
   int32_t* d_blocksT = nullptr;      // partition of T rows by T non-zeros
   int32_t* d_blocksN = nullptr;      // partition of N rows [0, NrowsN) by N non-zeros
   int32_t NrowBlocksT = 0, NrowBlocksN = 0;
+  // warp chunks ((r0, r1) pairs) for the T and N operators; counts are 0 when a
+  // row exceeds kWarpChunkNnz (the block kernels then serve every call)
+  int32_t* d_chunksT = nullptr;
+  int32_t* d_chunksN = nullptr;
+  int32_t nchunksT = 0, nchunksN = 0;
+  bool own_chunks_n = false;
+  int32_t chunk_order = 0;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
   bool own_blocks_n = false;      // d_blocksN is a separate allocation
 

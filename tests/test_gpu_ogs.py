@@ -180,3 +180,36 @@ def test_large_block_boundaries(cuda, orc):
     np.testing.assert_array_equal(
         host(dv), orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], v))
     assert h.info.maxRowSize == sizes.max()
+
+
+@pytest.mark.parametrize("kernel,order", [(0, 0), (1, 0), (1, 1)])
+@pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0)])
+def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
+    """Block kernels, and warp-chunk kernels in row and breadth-first order, all give
+    the reference's bits (each row is still summed by one lane in CSR order)."""
+    nx, ny, nz, p, seed = box
+    old = (capi.tune_get("ogs.kernel"), capi.tune_get("ogs.order"))
+    try:
+        capi.tune_set("ogs.kernel", kernel)
+        capi.tune_set("ogs.order", order)
+        ids = O.box_hex_ids(nx, ny, nz, p, seed)
+        h, ref = make(orc, ids)
+        assert h.info.chunkOrder == order and h.info.NchunksT > 0
+        rs, ci = ref["rsT"], ref["ciT"]
+        q = orc.uniform(ids.size, 91)
+        gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+        g = orc.uniform(rs.size - 1, 92)
+        dq = torch.zeros(ids.size, dtype=torch.float64, device="cuda")
+        h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)
+        np.testing.assert_array_equal(host(dq), orc.scatter(rs, ci, g, np.zeros(ids.size)))
+        dq = torch.from_numpy(q).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+        gN = torch.zeros(ref["rsN"].size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gN, torch.from_numpy(q).cuda(), 1, O.Add, O.NoTrans)
+        np.testing.assert_array_equal(host(gN), orc.gather(ref["rsN"], ref["ciN"], q))
+    finally:
+        capi.tune_set("ogs.kernel", old[0])
+        capi.tune_set("ogs.order", old[1])
