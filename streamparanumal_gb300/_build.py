@@ -90,6 +90,42 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+HOST = PKG / "host"
+BINDIR = PKG / "bin"
+BS_EXE = BINDIR / "spbs"
+
+
+def build_host(force: bool = False) -> Path:
+    """Compile the C++ mirror of the reference's platform_t / ogs_t / mesh_t
+    (host/libp, host/src) and the BS0-BS8 drivers (host/bs) into bin/spbs, linked
+    against libspgb300.so, with BS0 ... BS8 as links to it."""
+    cuda = _cuda_home()
+    srcs = sorted((HOST / "src").glob("*.cpp")) + sorted((HOST / "bs").glob("*.cpp"))
+    hdrs = sorted((HOST / "libp").glob("*.hpp")) + sorted((HOST / "bs").glob("*.hpp")) + \
+        [ROOT / "include" / "sp_capi.h"]
+    BINDIR.mkdir(parents=True, exist_ok=True)
+    if force or _stale(BS_EXE, srcs + hdrs + [LIB]):
+        obj_dir = BUILD / "host"
+        obj_dir.mkdir(parents=True, exist_ok=True)
+        inc = ["-I", str(ROOT / "include"), "-I", str(HOST / "libp"), "-I", str(HOST / "bs"),
+               "-I", str(cuda / "include")]
+        jobs = [["g++", "-O2", "-std=c++17", "-Wall", *inc, "-c", str(src), "-o",
+                 str(obj_dir / (src.parent.name + "_" + src.stem + ".o"))] for src in srcs]
+        with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+            list(ex.map(_run, jobs))
+        tmp = BS_EXE.with_suffix(".tmp")
+        _run(["g++", "-o", str(tmp), *[j[-1] for j in jobs], "-L", str(LIBDIR), "-lspgb300",
+              "-Wl,-rpath,$ORIGIN/../lib", "-L", str(cuda / "lib64"), "-lcudart",
+              f"-Wl,-rpath,{cuda / 'lib64'}"])
+        os.replace(tmp, BS_EXE)
+    for i in range(9):
+        link = BINDIR / f"BS{i}"
+        if link.is_symlink() or link.exists():
+            link.unlink()
+        link.symlink_to(BS_EXE.name)
+    return BS_EXE
+
+
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 
@@ -114,4 +150,5 @@ def build_oracle(force: bool = False) -> Path:
 
 if __name__ == "__main__":
     build_library(force=True, verbose=True)
+    build_host(force=True)
     build_oracle(force=True)
