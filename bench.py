@@ -416,6 +416,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
     # ---- BS0 launch latency: 10,000 empty launches, plain and graph-captured
     bs0 = bs0_latency(stream, dev)
+    # ---- FP32-storage forms and the full CG update (not part of `value`)
+    forms = storage_forms(stream, dev, h_a, h_b, h_q, h, N, Nt, Ng, per, alpha, beta)
 
     if rank != 0:
         return
@@ -444,7 +446,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "gpu_launches": launches,
         "clocks": clocks,
         "detail": {"per_kernel": detail, "bs0_us_per_launch": bs0,
-                   "setup_s": round(t_setup, 2)},
+                   "storage_forms": forms, "setup_s": round(t_setup, 2)},
     }
     if not args.no_cpu_baseline:
         gbs, desc, cores, _, _ = cpu_sample(args.cpu_nlog2, args.cpu_mesh, p, args.perm_seed,
@@ -454,6 +456,130 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
     if args.json_out:
         Path(args.json_out).write_text(json.dumps(line, indent=1))
+
+
+def _time(fn, stream, reps=10, warm=3) -> float:
+    """Mean device milliseconds of fn() over `reps` calls on `stream`."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def storage_forms(stream, dev, h_a, h_b, h_q, h, N, Nt, Ng, per, alpha, beta) -> dict:
+    """FP32-storage forms of BS1-BS8 and the full CG update (x += alpha p,
+    r -= alpha Ap, r.r), each against its FP64 form: device time, useful GB/s (the
+    FP64 byte accounting / time), bytes actually moved, and the error of every
+    result against the FP64 computation on the same FP64 inputs."""
+    import torch
+
+    from streamparanumal_gb300 import capi, kernels
+    from streamparanumal_gb300 import ogs as O
+
+    call = capi.call
+    sptr = stream.cuda_stream
+    out = {}
+    with torch.cuda.stream(stream):
+        a = h_a.to(dev, non_blocking=True)
+        b = h_b.to(dev, non_blocking=True)
+        a32, b32 = a.float(), b.float()
+        y32 = b32.clone()
+        res = torch.zeros(8, dtype=torch.float64, device=dev)
+        sc = kernels.ReduceScratch(dev)
+        f64 = {"BS1": 16 * N, "BS2": 24 * N, "BS3": 8 * N, "BS4": 16 * N}
+
+        def form(name, ms, actual, err=None):
+            d = {"ms": round(ms, 4), "useful_GBps": round(f64[name] / 1e6 / ms, 1),
+                 "actual_GBps": round(actual / 1e6 / ms, 1)}
+            if name in per:
+                d["speedup_vs_fp64"] = round(per[name] / ms, 3)
+            if err is not None:
+                d.update(err)
+            out[name] = d
+
+        form("BS1", _time(lambda: call("sp_bs1_copy_f32", N, a32.data_ptr(), y32.data_ptr(), sptr),
+                          stream), 8 * N)
+        form("BS2", _time(lambda: call("sp_bs2_axpy_f32", N, alpha, a32.data_ptr(), beta,
+                                       y32.data_ptr(), sptr), stream), 12 * N)
+        # BS3 / BS4: compensated FP32 lanes, FP64 finish
+        call("sp_norm2_f64", N, a.data_ptr(), res.data_ptr(), sc.ptr, sptr)
+        call("sp_dot_f64", N, a.data_ptr(), b.data_ptr(), res.data_ptr() + 8, sc.ptr, sptr)
+        a32d, b32d = a32.double(), b32.double()
+        call("sp_norm2_f64", N, a32d.data_ptr(), res.data_ptr() + 16, sc.ptr, sptr)
+        call("sp_dot_f64", N, a32d.data_ptr(), b32d.data_ptr(), res.data_ptr() + 24, sc.ptr, sptr)
+        del a32d, b32d
+        ms3 = _time(lambda: call("sp_norm2_f32", N, a32.data_ptr(), res.data_ptr() + 32, sc.ptr,
+                                 sptr), stream)
+        ms4 = _time(lambda: call("sp_dot_f32", N, a32.data_ptr(), b32.data_ptr(),
+                                 res.data_ptr() + 40, sc.ptr, sptr), stream)
+        r = res.cpu().tolist()
+        dot_scale = float((a * b).abs().sum())
+        form("BS3", ms3, 4 * N, {"rel_err_vs_fp64": abs(r[4] - r[0]) / abs(r[0]),
+                                 "rel_err_arith": abs(r[4] - r[2]) / abs(r[2])})
+        form("BS4", ms4, 8 * N, {"rel_err_vs_fp64": abs(r[5] - r[1]) / abs(r[1]),
+                                 "err_vs_fp64_over_sum_abs": abs(r[5] - r[1]) / dot_scale,
+                                 "rel_err_arith": abs(r[5] - r[3]) / abs(r[3])})
+        # full CG update: FP64 and FP32 storage
+        f64["CG"] = 48 * N
+        x, rr, p_, Ap = a.clone(), b.clone(), b.flip(0).contiguous(), a.flip(0).contiguous()
+        cg_alpha = 0.25
+        call("sp_cg_update_f64", N, cg_alpha, p_.data_ptr(), Ap.data_ptr(), x.data_ptr(),
+             rr.data_ptr(), res.data_ptr() + 48, sc.ptr, sptr)
+        x32, r32, p32, Ap32 = (t.float() for t in (a, b, p_, Ap))
+        call("sp_cg_update_f32", N, cg_alpha, p32.data_ptr(), Ap32.data_ptr(), x32.data_ptr(),
+             r32.data_ptr(), res.data_ptr() + 56, sc.ptr, sptr)
+        r = res.cpu().tolist()
+        xerr = float(((x32.double() - x).abs().max() / x.abs().max()))
+        ms64 = _time(lambda: call("sp_cg_update_f64", N, 1e-12, p_.data_ptr(), Ap.data_ptr(),
+                                  x.data_ptr(), rr.data_ptr(), res.data_ptr() + 48, sc.ptr, sptr),
+                     stream)
+        ms32 = _time(lambda: call("sp_cg_update_f32", N, 1e-12, p32.data_ptr(), Ap32.data_ptr(),
+                                  x32.data_ptr(), r32.data_ptr(), res.data_ptr() + 56, sc.ptr,
+                                  sptr), stream)
+        out["CG_fp64"] = {"ms": round(ms64, 4), "GBps": round(48 * N / 1e6 / ms64, 1)}
+        per["CG"] = ms64
+        form("CG", ms32, 24 * N, {"rdotr_rel_err_vs_fp64": abs(r[7] - r[6]) / abs(r[6]),
+                                  "x_max_rel_err_vs_fp64": xerr})
+        del x, rr, p_, Ap, x32, r32, p32, Ap32, a, b, a32, b32, y32
+        # BS6-BS8 on FP32 node data (same plan)
+        q = h_q.to(dev, non_blocking=True)
+        q32 = q.float()
+        g32 = torch.zeros(Ng, dtype=torch.float32, device=dev)
+        g64 = torch.zeros(Ng, dtype=torch.float64, device=dev)
+        f64.update({"BS6": (Ng + 1) * 4 + Nt * 4 + Nt * 8 + Ng * 8,
+                    "BS7": (Ng + 1) * 4 + Nt * 4 + Ng * 8 + Nt * 8,
+                    "BS8": (Ng + 1) * 4 + Nt * 4 + 2 * Nt * 8})
+        act = {"BS6": (Ng + 1) * 4 + Nt * 4 + Nt * 4 + Ng * 4,
+               "BS7": (Ng + 1) * 4 + Nt * 4 + Ng * 4 + Nt * 4,
+               "BS8": (Ng + 1) * 4 + Nt * 4 + 2 * Nt * 4}
+        h.Gather(g64, q, 1, O.Add, O.Trans, stream=stream)
+        h.Gather(g32, q32, 1, O.Add, O.Trans, stream=stream)
+        e6 = float((g32.double() - g64).abs().max() / g64.abs().max())
+        q64gs, q32gs = q.clone(), q32.clone()
+        h.GatherScatter(q64gs, 1, O.Add, O.Sym, stream=stream)
+        h.GatherScatter(q32gs, 1, O.Add, O.Sym, stream=stream)
+        e8 = float((q32gs.double() - q64gs).abs().max() / q64gs.abs().max())
+        del q64gs, q32gs
+        form("BS6", _time(lambda: h.Gather(g32, q32, 1, O.Add, O.Trans, stream=stream), stream),
+             act["BS6"], {"max_err_vs_fp64_over_max": e6})
+        form("BS7", _time(lambda: h.Scatter(q32, g32, 1, O.NoTrans, stream=stream), stream),
+             act["BS7"], {"exact_copy_of_fp32_values": True})
+        form("BS8", _time(lambda: h.GatherScatter(q32, 1, O.Add, O.Sym, stream=stream), stream),
+             act["BS8"], {"max_err_vs_fp64_over_max": e8})
+        del q, q32, g32, g64
+    torch.cuda.synchronize()
+    tot64 = sum(per[k] for k in ("BS1", "BS2", "BS3", "BS4", "BS6", "BS7", "BS8"))
+    tot32 = sum(out[k]["ms"] for k in ("BS1", "BS2", "BS3", "BS4", "BS6", "BS7", "BS8"))
+    out["suite_speedup_vs_fp64"] = round(tot64 / tot32, 3)
+    return out
 
 
 def bs0_latency(stream, dev) -> dict:

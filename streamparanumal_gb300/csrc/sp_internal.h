@@ -42,8 +42,9 @@ int sm_count();
 enum TuneKey : int {
   kTuneReducePrefetch = 0,  // order-exact reductions: L2 bulk-prefetch distance in chunks (0 = off)
   kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
-  kTuneOgsKernel,           // ogs: 0 = block kernels, 1 = warp-chunk kernels (k == 1 only)
+  kTuneOgsKernel,           // ogs: 0 block, 1 warp-chunk, 2 pipelined persistent warp-chunk (k == 1)
   kTuneOgsOrder,            // ogs plan: warp-chunk order, 0 = rows, 1 = breadth-first pages
+  kTuneReduceRolling,       // order-exact reductions: 1 = rolling load pipeline, 0 = grouped
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -229,13 +229,13 @@ __device__ __forceinline__ void warp_stage(const int32_t* __restrict__ ids, int3
 
 template <typename T, int OP>
 __global__ void __launch_bounds__(kOgsThreads, 6)
-k_ogsw_gs_sym(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+k_ogsw_gs_sym(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, T* __restrict__ v) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
-  const int2 ch = __ldg(chunks + c);
+  const int4 ch = __ldg(chunks + c);
   const int32_t nr = ch.y - ch.x;
   const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
   T* sv = sm.val[w];
@@ -258,13 +258,13 @@ k_ogsw_gs_sym(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* _
 
 template <typename T, int OP>
 __global__ void __launch_bounds__(kOgsThreads)
-k_ogsw_gather(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
-  const int2 ch = __ldg(chunks + c);
+  const int4 ch = __ldg(chunks + c);
   const int32_t nr = ch.y - ch.x;
   const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
   T* sv = sm.val[w];
@@ -283,13 +283,13 @@ k_ogsw_gather(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* _
 
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads)
-k_ogsw_scatter(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
                const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
-  const int2 ch = __ldg(chunks + c);
+  const int4 ch = __ldg(chunks + c);
   const int32_t nr = ch.y - ch.x;
   const int32_t s0 = __ldg(rs + ch.x), sn = __ldg(rs + ch.y) - s0;
   T* sv = sm.val[w];
@@ -310,12 +310,130 @@ k_ogsw_scatter(const int2* __restrict__ chunks, int32_t nchunks, const int32_t* 
     if (lane + 32 * u < sn) v[col[u]] = sv[lane + 32 * u];
 }
 
+// Persistent, software-pipelined variants (one warp walks chunks c, c+W, c+2W, ...):
+// the descriptor of chunk c+2W and the column ids of chunk c+W are loaded while
+// chunk c's gathers are in flight, so each chunk costs about one dependent memory
+// round trip instead of four.  Results are identical (same rows, same order).
+__device__ __forceinline__ void load_cols(const int32_t* __restrict__ ids, int4 d, int lane,
+                                          int32_t (&col)[kOgsPerLane]) {
+  const int32_t gn = d.w - d.z;
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u) {
+    const int i = lane + 32 * u;
+    col[u] = (i < gn) ? __ldg(ids + d.z + i) : 0;
+  }
+}
+
+template <typename T, int OP, int MODE>  // MODE 0: gather+scatter (Sym), 1: gather
+__global__ void __launch_bounds__(kOgsThreads, 4)
+k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv) {
+  __shared__ WarpSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  T* sv = sm.val[w];
+  int32_t* srs = sm.rs[w];
+  const int4 zero = make_int4(0, 0, 0, 0);
+  int4 d = __ldg(chunks + c);
+  int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  int32_t col[kOgsPerLane];
+  load_cols(ids, d, lane, col);
+  while (true) {
+    const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    const int32_t gn = d.w - d.z, nr = d.y - d.x;
+    T val[kOgsPerLane];
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) val[u] = v[col[u]];
+    for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + d.x + r) - d.z;
+    int32_t coln[kOgsPerLane];
+    load_cols(ids, dn, lane, coln);
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+    __syncwarp();
+    for (int32_t r = lane; r < nr; r += 32) {
+      const int32_t a = srs[r], b = srs[r + 1];
+      T acc = Op<T, OP>::init();
+      for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+      if (MODE == 0) {
+        for (int32_t i = a; i < b; ++i) sv[i] = acc;
+      } else {
+        gv[d.x + r] = acc;
+      }
+    }
+    __syncwarp();
+    if (MODE == 0) {
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u)
+        if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
+      __syncwarp();
+    }
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+    dn = dnn;
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u) col[u] = coln[u];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads, 4)
+k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v) {
+  __shared__ WarpSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  T* sv = sm.val[w];
+  const int4 zero = make_int4(0, 0, 0, 0);
+  int4 d = __ldg(chunks + c);
+  int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  int32_t col[kOgsPerLane];
+  load_cols(ids, d, lane, col);
+  while (true) {
+    const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    const int32_t sn = d.w - d.z, nr = d.y - d.x;
+    int32_t coln[kOgsPerLane];
+    load_cols(ids, dn, lane, coln);
+    for (int32_t r = lane; r < nr; r += 32) {
+      const T x = gv[d.x + r];
+      const int32_t a = __ldg(rs + d.x + r) - d.z, b = __ldg(rs + d.x + r + 1) - d.z;
+      for (int32_t i = a; i < b; ++i) sv[i] = x;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < sn) v[col[u]] = sv[lane + 32 * u];
+    __syncwarp();
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+    dn = dnn;
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u) col[u] = coln[u];
+  }
+}
+
+static inline unsigned persistent_grid(int32_t nchunks) {
+  const int64_t want = ((int64_t)nchunks + kWarpsPerCta - 1) / kWarpsPerCta;
+  const int64_t cap = (int64_t)sm_count() * 4;
+  return (unsigned)(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
 static inline unsigned warp_grid(int32_t nchunks) {
   return (unsigned)((nchunks + kWarpsPerCta - 1) / kWarpsPerCta);
 }
 
 static inline bool use_warp(const sp_ogs_plan* p, int K, int32_t nchunks) {
   return K == 1 && nchunks > 0 && tune(kTuneOgsKernel) == 1;
+}
+static inline bool use_pipe(const sp_ogs_plan* p, int K, int32_t nchunks) {
+  return K == 1 && nchunks > 0 && tune(kTuneOgsKernel) == 2;
 }
 
 // ------------------------------------------------------------------ dispatch
@@ -324,9 +442,13 @@ template <typename T, int OP>
 static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
-  if ((trans == SP_SYM || p->n_is_t) && use_warp(p, K, p->nchunksT)) {
+  if ((trans == SP_SYM || p->n_is_t) && use_pipe(p, K, p->nchunksT)) {
+    k_ogsp_gather<T, OP, 0><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        v, nullptr);
+  } else if ((trans == SP_SYM || p->n_is_t) && use_warp(p, K, p->nchunksT)) {
     k_ogsw_gs_sym<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT, v);
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT, v);
   } else if (trans == SP_SYM || p->n_is_t) {
     k_ogs_gs_sym<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
                                                      v, K);
@@ -343,13 +465,21 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
 template <typename T, int OP>
 static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
                           cudaStream_t s) {
-  if (trans == SP_NOTRANS && use_warp(p, K, p->nchunksN)) {
+  if (trans == SP_NOTRANS && use_pipe(p, K, p->nchunksN)) {
+    k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        p->d_colIdsN, const_cast<T*>(v), gv);
+  } else if (trans != SP_NOTRANS && use_pipe(p, K, p->nchunksT)) {
+    k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        const_cast<T*>(v), gv);
+  } else if (trans == SP_NOTRANS && use_warp(p, K, p->nchunksN)) {
     k_ogsw_gather<T, OP><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int2*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, v, gv);
   } else if (trans != SP_NOTRANS && use_warp(p, K, p->nchunksT)) {
     k_ogsw_gather<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         v, gv);
   } else if (trans == SP_NOTRANS) {
     if (p->NrowBlocksN == 0) return;
@@ -365,13 +495,21 @@ static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv
 template <typename T>
 static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, const T* gv,
                            cudaStream_t s) {
-  if (trans == SP_TRANS && use_warp(p, K, p->nchunksN)) {
+  if (trans == SP_TRANS && use_pipe(p, K, p->nchunksN)) {
+    k_ogsp_scatter<T><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        p->d_colIdsN, gv, v);
+  } else if (trans != SP_TRANS && use_pipe(p, K, p->nchunksT)) {
+    k_ogsp_scatter<T><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        gv, v);
+  } else if (trans == SP_TRANS && use_warp(p, K, p->nchunksN)) {
     k_ogsw_scatter<T><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int2*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, gv, v);
   } else if (trans != SP_TRANS && use_warp(p, K, p->nchunksT)) {
     k_ogsw_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int2*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         gv, v);
   } else if (trans == SP_TRANS) {
     if (p->NrowBlocksN == 0) return;
@@ -567,8 +705,22 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
                    chunksN)) {
     p->nchunksT = (int32_t)(chunksT.size() / 2);
     p->nchunksN = (int32_t)(chunksN.size() / 2);
+    // descriptors (r0, r1, g0, g1): the entry range rides along with the row range
+    auto quads = [](const std::vector<int32_t>& pairs, const std::vector<int32_t>& rs) {
+      std::vector<int32_t> q(pairs.size() * 2);
+      for (size_t c = 0; c < pairs.size() / 2; ++c) {
+        q[4 * c + 0] = pairs[2 * c];
+        q[4 * c + 1] = pairs[2 * c + 1];
+        q[4 * c + 2] = rs[pairs[2 * c]];
+        q[4 * c + 3] = rs[pairs[2 * c + 1]];
+      }
+      return q;
+    };
+    const bool same = (chunksN == chunksT);
+    chunksT = quads(chunksT, p->rowStartsT);
+    chunksN = same ? chunksT : quads(chunksN, p->rowStartsN);
     if ((st = upload(chunksT, &p->d_chunksT, s))) return st;
-    if (chunksN == chunksT) {
+    if (same) {
       p->d_chunksN = p->d_chunksT;
     } else {
       p->own_chunks_n = true;

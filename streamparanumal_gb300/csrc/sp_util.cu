@@ -33,8 +33,9 @@ struct TuneEntry {
 static TuneEntry g_tune[kTuneCount] = {
     {"reduce.prefetch_chunks", 0, 64, {4}},
     {"ogs.block_nnz", 256, 2048, {2048}},
-    {"ogs.kernel", 0, 1, {1}},
+    {"ogs.kernel", 0, 2, {1}},
     {"ogs.order", 0, 1, {1}},
+    {"reduce.rolling", 0, 1, {1}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

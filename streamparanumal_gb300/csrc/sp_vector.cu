@@ -220,7 +220,11 @@ __device__ __forceinline__ void prefetch_chunk(const double* x, int64_t base, in
   if (bytes) prefetch_l2(x + start, bytes);
 }
 
-template <int BS, int U>
+// ROLL = true keeps U loads in flight at all times: each value is replaced by the
+// load of the same lane slot of the next group as soon as it has been read, and
+// the in-order accumulation then waits on the older loads only.  ROLL = false
+// loads a group, consumes it, loads the next.  Both add in the same order.
+template <int BS, int U, bool ROLL>
 __global__ void __launch_bounds__(BS)
 k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict__ partial,
         int pd) {
@@ -232,13 +236,34 @@ k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict
   if (pf && t < pd) prefetch_chunk<BS>(a, base, stride, t, n);
   int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
-    if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
-    double v[U];
+  if (ROLL) {
+    if (id + (U - 1) * stride < n) {
+      double v[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) v[u] = __ldcs(a + id + u * stride);
+      for (int u = 0; u < U; ++u) v[u] = __ldcs(a + id + u * stride);
+      id += U * stride;
+      j += U;
+      for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+        if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
 #pragma unroll
-    for (int u = 0; u < U; ++u) acc = fma(v[u], v[u], acc);
+        for (int u = 0; u < U; ++u) {
+          const double x = v[u];
+          v[u] = __ldcs(a + id + u * stride);
+          acc = fma(x, x, acc);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fma(v[u], v[u], acc);
+    }
+  } else {
+    for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+      if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
+      double v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) v[u] = __ldcs(a + id + u * stride);
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fma(v[u], v[u], acc);
+    }
   }
   for (; id < n; id += stride) {
     const double v = __ldcs(a + id);
@@ -248,7 +273,7 @@ k_bs3_1(int nblocks, int64_t n, const double* __restrict__ a, double* __restrict
   if (t == 0) partial[blockIdx.x] = r;
 }
 
-template <int BS, int U>
+template <int BS, int U, bool ROLL>
 __global__ void __launch_bounds__(BS)
 k_bs4_1(int nblocks, int64_t n, const double* __restrict__ a, const double* __restrict__ b,
         double* __restrict__ partial, int pd) {
@@ -262,24 +287,50 @@ k_bs4_1(int nblocks, int64_t n, const double* __restrict__ a, const double* __re
   if (pf && t >= 32 && t < 32 + pd) prefetch_chunk<BS>(b, base, stride, t - 32, n);
   int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
-    if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
-    if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(b, base, stride, j + pd + t - 32, n);
-    double va[U], vb[U];
+  if (ROLL) {
+    if (id + (U - 1) * stride < n) {
+      double va[U], vb[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      va[u] = __ldcs(a + id + u * stride);
-      vb[u] = __ldcs(b + id + u * stride);
+      for (int u = 0; u < U; ++u) {
+        va[u] = __ldcs(a + id + u * stride);
+        vb[u] = __ldcs(b + id + u * stride);
+      }
+      id += U * stride;
+      j += U;
+      for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+        if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
+        if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(b, base, stride, j + pd + t - 32, n);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const double x = va[u], y = vb[u];
+          va[u] = __ldcs(a + id + u * stride);
+          vb[u] = __ldcs(b + id + u * stride);
+          acc = fma(x, y, acc);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fma(va[u], vb[u], acc);
     }
+  } else {
+    for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+      if (pf && t < U) prefetch_chunk<BS>(a, base, stride, j + pd + t, n);
+      if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(b, base, stride, j + pd + t - 32, n);
+      double va[U], vb[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) acc = fma(va[u], vb[u], acc);
+      for (int u = 0; u < U; ++u) {
+        va[u] = __ldcs(a + id + u * stride);
+        vb[u] = __ldcs(b + id + u * stride);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fma(va[u], vb[u], acc);
+    }
   }
   for (; id < n; id += stride) acc = fma(__ldcs(a + id), __ldcs(b + id), acc);
   const double r = tree_reduce<BS>(acc, s);
   if (t == 0) partial[blockIdx.x] = r;
 }
 
-template <int BS, int U>
+template <int BS, int U, bool ROLL>
 __global__ void __launch_bounds__(BS)
 k_bs5_1(int nblocks, int64_t n, const double* __restrict__ Ap, double alpha, double* __restrict__ r,
         double* __restrict__ partial, int pd) {
@@ -293,20 +344,52 @@ k_bs5_1(int nblocks, int64_t n, const double* __restrict__ Ap, double alpha, dou
   if (pf && t >= 32 && t < 32 + pd) prefetch_chunk<BS>(Ap, base, stride, t - 32, n);
   int64_t id = base + t, j = 0;
   double acc = 0.0;
-  for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
-    if (pf && t < U) prefetch_chunk<BS>(r, base, stride, j + pd + t, n);
-    if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(Ap, base, stride, j + pd + t - 32, n);
-    double vr[U], va[U];
+  if (ROLL) {
+    if (id + (U - 1) * stride < n) {
+      double vr[U], va[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      vr[u] = __ldcs(r + id + u * stride);
-      va[u] = __ldcs(Ap + id + u * stride);
+      for (int u = 0; u < U; ++u) {
+        vr[u] = __ldcs(r + id + u * stride);
+        va[u] = __ldcs(Ap + id + u * stride);
+      }
+      int64_t prev = id;
+      id += U * stride;
+      j += U;
+      for (; id + (U - 1) * stride < n; prev = id, id += U * stride, j += U) {
+        if (pf && t < U) prefetch_chunk<BS>(r, base, stride, j + pd + t, n);
+        if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(Ap, base, stride, j + pd + t - 32, n);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const double rr = fma(alpha, va[u], vr[u]);
+          vr[u] = __ldcs(r + id + u * stride);
+          va[u] = __ldcs(Ap + id + u * stride);
+          __stcs(r + prev + u * stride, rr);
+          acc = fma(rr, rr, acc);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const double rr = fma(alpha, va[u], vr[u]);
+        __stcs(r + prev + u * stride, rr);
+        acc = fma(rr, rr, acc);
+      }
     }
+  } else {
+    for (; id + (U - 1) * stride < n; id += U * stride, j += U) {
+      if (pf && t < U) prefetch_chunk<BS>(r, base, stride, j + pd + t, n);
+      if (pf && t >= 32 && t < 32 + U) prefetch_chunk<BS>(Ap, base, stride, j + pd + t - 32, n);
+      double vr[U], va[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const double rr = fma(alpha, va[u], vr[u]);
-      __stcs(r + id + u * stride, rr);
-      acc = fma(rr, rr, acc);
+      for (int u = 0; u < U; ++u) {
+        vr[u] = __ldcs(r + id + u * stride);
+        va[u] = __ldcs(Ap + id + u * stride);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const double rr = fma(alpha, va[u], vr[u]);
+        __stcs(r + id + u * stride, rr);
+        acc = fma(rr, rr, acc);
+      }
     }
   }
   for (; id < n; id += stride) {
@@ -329,6 +412,46 @@ k_finish(int nblocks, const double* __restrict__ partial, double* __restrict__ o
   if (t < nblocks) v = 0.0 + partial[t];
   const double r = tree_reduce<BS>(v, s);
   if (t == 0) out[0] = r;
+}
+
+// Launch helpers of the stage-1 kernels: U per block size, ROLL from the tuning knob.
+template <bool R>
+static void launch_bs3_impl(int bs, int nb, int64_t n, const double* a, double* part, int pd,
+                            cudaStream_t s) {
+  if (bs == 256) k_bs3_1<256, 16, R><<<nb, 256, 0, s>>>(nb, n, a, part, pd);
+  else if (bs == 512) k_bs3_1<512, 8, R><<<nb, 512, 0, s>>>(nb, n, a, part, pd);
+  else k_bs3_1<1024, 4, R><<<nb, 1024, 0, s>>>(nb, n, a, part, pd);
+}
+template <bool R>
+static void launch_bs4_impl(int bs, int nb, int64_t n, const double* a, const double* b,
+                            double* part, int pd, cudaStream_t s) {
+  if (bs == 256) k_bs4_1<256, 8, R><<<nb, 256, 0, s>>>(nb, n, a, b, part, pd);
+  else if (bs == 512) k_bs4_1<512, 4, R><<<nb, 512, 0, s>>>(nb, n, a, b, part, pd);
+  else k_bs4_1<1024, 4, R><<<nb, 1024, 0, s>>>(nb, n, a, b, part, pd);
+}
+template <bool R>
+static void launch_bs5_impl(int bs, int nb, int64_t n, const double* Ap, double alpha, double* r,
+                            double* part, int pd, cudaStream_t s) {
+  if (bs == 256) k_bs5_1<256, 8, R><<<nb, 256, 0, s>>>(nb, n, Ap, alpha, r, part, pd);
+  else if (bs == 512) k_bs5_1<512, 4, R><<<nb, 512, 0, s>>>(nb, n, Ap, alpha, r, part, pd);
+  else k_bs5_1<1024, 4, R><<<nb, 1024, 0, s>>>(nb, n, Ap, alpha, r, part, pd);
+}
+static void launch_bs3(int bs, int nb, int64_t n, const double* a, double* part, cudaStream_t s) {
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (tune(kTuneReduceRolling)) launch_bs3_impl<true>(bs, nb, n, a, part, pd, s);
+  else launch_bs3_impl<false>(bs, nb, n, a, part, pd, s);
+}
+static void launch_bs4(int bs, int nb, int64_t n, const double* a, const double* b, double* part,
+                       cudaStream_t s) {
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (tune(kTuneReduceRolling)) launch_bs4_impl<true>(bs, nb, n, a, b, part, pd, s);
+  else launch_bs4_impl<false>(bs, nb, n, a, b, part, pd, s);
+}
+static void launch_bs5(int bs, int nb, int64_t n, const double* Ap, double alpha, double* r,
+                       double* part, cudaStream_t s) {
+  const int pd = (int)tune(kTuneReducePrefetch);
+  if (tune(kTuneReduceRolling)) launch_bs5_impl<true>(bs, nb, n, Ap, alpha, r, part, pd, s);
+  else launch_bs5_impl<false>(bs, nb, n, Ap, alpha, r, part, pd, s);
 }
 
 static sp_status check_exact_args(int32_t bs, int32_t nblocks, int64_t n, const char* name) {
@@ -659,10 +782,7 @@ sp_status sp_bs3_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, 
   if (st) return st;
   if (!partial || (n > 0 && !a)) return fail(SP_ERR_INVALID_ARG, "sp_bs3_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  const int pd = (int)tune(kTuneReducePrefetch);
-  if (bs == 256) k_bs3_1<256, 16><<<nblocks, 256, 0, s>>>(nblocks, n, a, partial, pd);
-  else if (bs == 512) k_bs3_1<512, 8><<<nblocks, 512, 0, s>>>(nblocks, n, a, partial, pd);
-  else k_bs3_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, partial, pd);
+  launch_bs3(bs, nblocks, n, a, partial, s);
   return check_launch("sp_bs3_1_f64");
 }
 
@@ -673,10 +793,7 @@ sp_status sp_bs4_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a, 
   if (!partial || (n > 0 && (!a || !b)))
     return fail(SP_ERR_INVALID_ARG, "sp_bs4_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  const int pd = (int)tune(kTuneReducePrefetch);
-  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial, pd);
-  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial, pd);
-  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial, pd);
+  launch_bs4(bs, nblocks, n, a, b, partial, s);
   return check_launch("sp_bs4_1_f64");
 }
 
@@ -687,10 +804,7 @@ sp_status sp_bs5_1_f64(int32_t bs, int32_t nblocks, int64_t n, const double* Ap,
   if (!partial || (n > 0 && (!Ap || !r)))
     return fail(SP_ERR_INVALID_ARG, "sp_bs5_1_f64: null pointer");
   cudaStream_t s = as_cuda(stream);
-  const int pd = (int)tune(kTuneReducePrefetch);
-  if (bs == 256) k_bs5_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
-  else if (bs == 512) k_bs5_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
-  else k_bs5_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, Ap, alpha, r, partial, pd);
+  launch_bs5(bs, nblocks, n, Ap, alpha, r, partial, s);
   return check_launch("sp_bs5_1_f64");
 }
 
@@ -895,10 +1009,7 @@ sp_status sp_bs4_dot_f64_noalloc(int32_t bs, int32_t nblocks, int64_t n, const d
   // stage 1 writes partial[0, nblocks) in full before stage 2 reads it, so nothing
   // in the shared array has to start at zero
   cudaStream_t s = as_cuda(stream);
-  const int pd = (int)tune(kTuneReducePrefetch);
-  if (bs == 256) k_bs4_1<256, 8><<<nblocks, 256, 0, s>>>(nblocks, n, a, b, partial, pd);
-  else if (bs == 512) k_bs4_1<512, 4><<<nblocks, 512, 0, s>>>(nblocks, n, a, b, partial, pd);
-  else k_bs4_1<1024, 4><<<nblocks, 1024, 0, s>>>(nblocks, n, a, b, partial, pd);
+  launch_bs4(bs, nblocks, n, a, b, partial, s);
   if ((st = check_launch("sp_bs4_dot_f64_noalloc"))) return st;
   if (bs == 256) k_finish<256><<<1, 256, 0, s>>>(nblocks, partial, out);
   else if (bs == 512) k_finish<512><<<1, 512, 0, s>>>(nblocks, partial, out);

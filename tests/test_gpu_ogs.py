@@ -182,7 +182,7 @@ def test_large_block_boundaries(cuda, orc):
     assert h.info.maxRowSize == sizes.max()
 
 
-@pytest.mark.parametrize("kernel,order", [(0, 0), (1, 0), (1, 1)])
+@pytest.mark.parametrize("kernel,order", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
 @pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0)])
 def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
     """Block kernels, and warp-chunk kernels in row and breadth-first order, all give
