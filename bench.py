@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--cpu-nlog2", type=int, default=24)
     ap.add_argument("--cpu-mesh", type=int, default=32)
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--batch", action="store_true",
+                    help="the batched workload: 256 uneven instances (CG update + BS8 each), "
+                         "one persistent launch vs per-instance launches, plain and graphed")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-emax", type=int, default=40)
     ap.add_argument("--kernels-only", action="store_true",
                     help="time the suite only (no e2e, BS0, clock soak or CPU leg): for ncu")
     return ap.parse_args()
@@ -614,6 +619,91 @@ def bs0_latency(stream, dev) -> dict:
     return {"plain": round(plain, 3), "graph": round(graph, 3), "launches": n}
 
 
+def run_batch(args, local_rank: int) -> None:
+    """Batched uneven workload: instance i has an Ex*Ey*Ez hex box (each in
+    [2, emax]) of degree p in [2, 9] (seeded), a CG update on its own x, r, p, Ap
+    (n = its local nodes) and a BS8 gather+scatter on its own q.  Timed four ways:
+    per-instance launches (2 per instance), the same launches replayed from one CUDA
+    graph, one persistent batched launch, and that launch replayed from a graph."""
+    import numpy as np
+    import torch
+
+    from streamparanumal_gb300 import _build, batch, capi, kernels
+    from streamparanumal_gb300 import ogs as O
+
+    _build.build_library()
+    capi.load()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    rng = np.random.default_rng(args.seed)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(args.seed)
+    stream = torch.cuda.Stream(device=dev)
+    t0 = time.time()
+    plans, vecs, alphas, sizes = [], [], [], []
+    with torch.cuda.stream(stream):
+        for i in range(args.batch_count):
+            ex, ey, ez = (int(v) for v in rng.integers(2, args.batch_emax + 1, size=3))
+            p = int(rng.integers(2, 10))
+            ids = O.box_hex_ids(ex, ey, ez, p, int(rng.integers(1, 1 << 30)))
+            h = O.ogs_t()
+            h.Setup(ids.size, ids, unique=True, stream=stream)
+            n = ids.size
+            v = {k: torch.rand(n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+                 for k in ("x", "r", "p", "Ap", "q")}
+            v["rr"] = torch.zeros(1, dtype=torch.float64, device=dev)
+            plans.append(h)
+            vecs.append(v)
+            alphas.append(float(rng.uniform(-1, 1)) * 1e-3)
+            sizes.append((ex, ey, ez, p, n, h.NgatherGlobal))
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    sc = kernels.ReduceScratch(dev)
+    sptr = stream.cuda_stream
+
+    def per_instance():
+        for h, v, a in zip(plans, vecs, alphas):
+            capi.call("sp_cg_update_f64", v["x"].numel(), a, v["p"].data_ptr(), v["Ap"].data_ptr(),
+                      v["x"].data_ptr(), v["r"].data_ptr(), v["rr"].data_ptr(), sc.ptr, sptr)
+            capi.call("sp_ogs_gather_scatter", h._plan, capi.DOUBLE, capi.ADD, capi.SYM, 1,
+                      v["q"].data_ptr(), sptr)
+
+    b = batch.Batch(plans, [v["x"] for v in vecs], [v["r"] for v in vecs],
+                    [v["p"] for v in vecs], [v["Ap"] for v in vecs], [v["rr"] for v in vecs],
+                    [v["q"] for v in vecs], alphas, stream=stream)
+    with torch.cuda.stream(stream):
+        g_inst = batch.Graph(stream)
+        with g_inst:
+            per_instance()
+        g_batch = batch.Graph(stream)
+        with g_batch:
+            b.run(stream=stream)
+    reps = max(3, min(args.steps, 20))
+    res = {"per_instance_launches": _time(per_instance, stream, reps),
+           "per_instance_graph": _time(lambda: g_inst.launch(), stream, reps),
+           "batched_persistent": _time(lambda: b.run(stream=stream), stream, reps),
+           "batched_graph": _time(lambda: g_batch.launch(), stream, reps)}
+    nodes = sum(x[4] for x in sizes)
+    ng = sum(x[5] for x in sizes)
+    nbytes = 48 * nodes + (ng + len(sizes)) * 4 + nodes * 4 + 16 * nodes
+    per = {k: round(v / len(sizes) * 1e3, 3) for k, v in res.items()}  # us per instance
+    line = {"metric": "batched CG update + BS8 per-instance time", "unit": "us/instance",
+            "value": per["batched_graph"], "higher_is_better": False, "n_gpus": 1,
+            "steps": reps, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(sizes)} instances, Ex,Ey,Ez in [2,{args.batch_emax}], "
+                                   f"p in [2,9]", "local_nodes": nodes, "global_nodes": ng},
+            "per_instance_us": per,
+            "speedup_batched_graph_vs_launches": round(res["per_instance_launches"]
+                                                       / res["batched_graph"], 3),
+            "GBps_batched": round(nbytes / 1e6 / res["batched_persistent"], 1),
+            "GBps_per_instance_launches": round(nbytes / 1e6 / res["per_instance_launches"], 1),
+            "launches": {"per_instance": 2 * len(sizes), "batched": 1},
+            "setup_s": round(setup_s, 1)}
+    print(json.dumps(line), flush=True)
+    if args.json_out:
+        Path(args.json_out).write_text(json.dumps(line, indent=1))
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -621,6 +711,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.batch:
+        if rank == 0:
+            run_batch(args, local_rank)
         return
     if world > 1:
         import torch

@@ -80,6 +80,11 @@ sp_status sp_bs0(int32_t n, const double* a, double* b, sp_stream_t stream);
 typedef struct sp_graph sp_graph;
 sp_status sp_bs0_graph_create(int32_t nlaunches, int32_t n, const double* a, double* b,
                               sp_stream_t stream, sp_graph** out);
+/* Capture everything this host thread launches on `stream` (a created stream, not
+ * the legacy default one) between sp_graph_begin and sp_graph_end into one graph;
+ * replay it with sp_graph_launch.  Plans and buffers must exist before capture. */
+sp_status sp_graph_begin(sp_stream_t stream);
+sp_status sp_graph_end(sp_stream_t stream, sp_graph** out);
 sp_status sp_graph_launch(const sp_graph* g, sp_stream_t stream);
 sp_status sp_graph_destroy(sp_graph* g);
 
@@ -236,6 +241,24 @@ sp_status sp_ogs_scatter(const sp_ogs_plan* plan, sp_type type, sp_transpose tra
                          void* v, const void* gv, sp_stream_t stream);
 sp_status sp_ogs_gather_scatter(const sp_ogs_plan* plan, sp_type type, sp_op op,
                                 sp_transpose trans, int32_t k, void* v, sp_stream_t stream);
+
+/* ---------------------------------------------------------------- batched instances
+ * Many independent instances of uneven size in ONE persistent launch.  Instance i
+ * owns x[i], r[i], p[i], Ap[i] (n[i] doubles), rdotr[i] (one double) and alpha[i],
+ * and a node field q[i] with its own plan.  sp_batch_run performs, for every i,
+ *   x += alpha p;  r -= alpha Ap;  rdotr = r.r      (values of sp_cg_update_f64;
+ *                                                     r.r in its own fixed order)
+ *   q <- GatherScatter(q, Add, Sym)                 (bits of sp_ogs_gather_scatter)
+ * Arrays of device pointers are read at creation (host arrays); the plans must
+ * outlive the batch and have warp chunks (every group <= 256 members).  Runs of one
+ * batch must not overlap on the device (they share per-instance tickets). */
+typedef struct sp_batch sp_batch;
+sp_status sp_batch_create(int32_t ninst, const sp_ogs_plan* const* plans, const int64_t* n,
+                          double* const* x, double* const* r, const double* const* p,
+                          const double* const* Ap, double* const* rdotr, double* const* q,
+                          const double* alpha, sp_stream_t stream, sp_batch** out);
+sp_status sp_batch_run(const sp_batch* b, sp_stream_t stream);
+sp_status sp_batch_destroy(sp_batch* b);
 
 /* ---------------------------------------------------------------- box mesh ids
  * Global node ids of a structured nx*ny*nz hex box of degree p on one rank, as

@@ -1,0 +1,110 @@
+"""Per-degree autotuner of the gather-scatter launch configuration.
+
+For a hex box of degree p it times BS6 (Gather Trans), BS7 (Scatter NoTrans) and
+BS8 (GatherScatter Sym) under every compiled variant -- block kernels (rows cut into
+blocks of `ogs.block_nnz` entries), warp-chunk kernels and pipelined persistent
+warp-chunk kernels, each with chunks in row order or breadth-first page order --
+and keeps the fastest by total time.  Results are stored per degree in a JSON table
+(`tuning/gb300.json` by default) that :func:`apply` loads into the library's tuning
+knobs before plans are built.  Every variant computes the same bits; only speed
+differs.
+"""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import torch
+
+from . import capi
+from . import ogs as O
+
+TABLE = Path(__file__).resolve().parent / "tuning" / "gb300.json"
+
+# (plan-time knobs) x (launch-time kernel): plans are rebuilt only when order or
+# block_nnz change
+PLAN_CONFIGS = [{"order": 1, "block_nnz": 2048}, {"order": 0, "block_nnz": 2048},
+                {"order": 0, "block_nnz": 1024}]
+KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined"}
+
+
+def _time(fn, reps: int, stream) -> float:
+    for _ in range(2):
+        fn()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _set(cfg: dict) -> None:
+    capi.tune_set("ogs.order", cfg["order"])
+    capi.tune_set("ogs.block_nnz", cfg["block_nnz"])
+    capi.tune_set("ogs.kernel", cfg["kernel"])
+
+
+def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
+             ids=None) -> dict:
+    """Times every variant on an E^3 box of degree p; returns the winner and all
+    timings (ms per call)."""
+    saved = {k: capi.tune_get(f"ogs.{k}") for k in ("order", "block_nnz", "kernel")}
+    stream = torch.cuda.current_stream()
+    if ids is None:
+        ids = O.box_hex_ids(E, E, E, p, perm_seed)
+    Nt = ids.size
+    q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
+    results = []
+    try:
+        for pc in PLAN_CONFIGS:
+            _set({**pc, "kernel": 1})
+            h = O.ogs_t()
+            h.Setup(Nt, ids.copy(), unique=True)
+            gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
+            kernels = [0] if pc["order"] == 0 else []
+            kernels += [1, 2] if pc["block_nnz"] == 2048 else []
+            for k in kernels:
+                capi.tune_set("ogs.kernel", k)
+                t6 = _time(lambda: h.Gather(gq, q, 1, O.Add, O.Trans), reps, stream)
+                t7 = _time(lambda: h.Scatter(q, gq, 1, O.NoTrans), reps, stream)
+                t8 = _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), reps, stream)
+                results.append({**pc, "kernel": k, "ms": {"BS6": t6, "BS7": t7, "BS8": t8},
+                                "total_ms": t6 + t7 + t8})
+            h.Free()
+            del gq
+    finally:
+        _set(saved)
+    best = min(results, key=lambda r: r["total_ms"])
+    return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt),
+            "best": {k: best[k] for k in ("kernel", "order", "block_nnz")},
+            "candidates": results}
+
+
+def load_table(path: Path = TABLE) -> dict:
+    if path.exists():
+        return json.loads(path.read_text())
+    return {}
+
+
+def save_table(table: dict, path: Path = TABLE) -> None:
+    path.parent.mkdir(parents=True, exist_ok=True)
+    path.write_text(json.dumps(table, indent=1, sort_keys=True) + "\n")
+
+
+def record(table: dict, result: dict) -> None:
+    """Stores a tune_ogs() winner under its degree (and layout)."""
+    key = f"p{result['p']}" + ("_perm" if result["perm"] else "")
+    table[key] = result["best"]
+
+
+def apply(p: int, perm: bool = False, table: dict | None = None) -> dict:
+    """Sets the ogs knobs for degree p from the table (library defaults when the
+    degree is not tuned); plans created afterwards use them."""
+    table = load_table() if table is None else table
+    cfg = table.get(f"p{p}" + ("_perm" if perm else "")) or table.get(f"p{p}")
+    if cfg:
+        _set(cfg)
+    return cfg or {}

@@ -64,6 +64,8 @@ SIGNATURES = {
     "sp_tune_get": (c_int32, [ctypes.c_char_p, _I64P]),
     "sp_bs0": (c_int32, [c_int32, _P, _P, _P]),
     "sp_bs0_graph_create": (c_int32, [c_int32, c_int32, _P, _P, _P, POINTER(c_void_p)]),
+    "sp_graph_begin": (c_int32, [_P]),
+    "sp_graph_end": (c_int32, [_P, POINTER(c_void_p)]),
     "sp_graph_launch": (c_int32, [_P, _P]),
     "sp_graph_destroy": (c_int32, [_P]),
     "sp_bs1_copy_f64": (c_int32, [c_int64, _P, _P, _P]),
@@ -94,6 +96,10 @@ SIGNATURES = {
     "sp_ogs_gather": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P, _P]),
     "sp_ogs_scatter": (c_int32, [_P, c_int32, c_int32, c_int32, _P, _P, _P]),
     "sp_ogs_gather_scatter": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P]),
+    "sp_batch_create": (c_int32, [c_int32, _P, _I64P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                  POINTER(c_void_p)]),
+    "sp_batch_run": (c_int32, [_P, _P]),
+    "sp_batch_destroy": (c_int32, [_P]),
     "sp_mesh_box_hex_ids": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _I64P]),
 }
 

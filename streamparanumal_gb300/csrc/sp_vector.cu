@@ -899,6 +899,8 @@ sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float*
 
 }  // extern "C"
 
+static thread_local int64_t g_capture_start = 0;
+
 struct sp_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -930,6 +932,34 @@ sp_status sp_bs0_graph_create(int32_t nlaunches, int32_t n, const double* a, dou
     delete g;
     return fail(SP_ERR_CUDA, "sp_bs0_graph_create: %s", cudaGetErrorString(e));
   }
+  *out = g;
+  return SP_SUCCESS;
+}
+
+sp_status sp_graph_begin(sp_stream_t stream) {
+  if (!stream) return fail(SP_ERR_INVALID_ARG, "sp_graph_begin: capture needs a created stream");
+  SP_CUDA_TRY(cudaStreamBeginCapture(as_cuda(stream), cudaStreamCaptureModeThreadLocal));
+  g_capture_start = sp_launch_count();
+  return SP_SUCCESS;
+}
+
+sp_status sp_graph_end(sp_stream_t stream, sp_graph** out) {
+  if (!stream || !out) return fail(SP_ERR_INVALID_ARG, "sp_graph_end: null argument");
+  *out = nullptr;
+  sp_graph* g = new sp_graph();
+  cudaError_t e = cudaStreamEndCapture(as_cuda(stream), &g->graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e == cudaSuccess) e = cudaGraphUpload(g->exec, as_cuda(stream));
+  if (e != cudaSuccess) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    cudaGetLastError();
+    return fail(SP_ERR_CUDA, "sp_graph_end: %s", cudaGetErrorString(e));
+  }
+  g->nlaunches = (int32_t)(sp_launch_count() - g_capture_start);
+  // launches recorded into the graph ran nothing yet: count them when it is replayed
+  count_launch(-(int64_t)g->nlaunches);
   *out = g;
   return SP_SUCCESS;
 }

@@ -69,7 +69,10 @@ def test_bs1_to_bs5_rows(cuda, bsdir, which, title, extra):
     lines = out.strip().split("\n")
     assert lines[0] == f"%{title} [DOFs, elapsed, DOFs/s, BW (GB/s)]"
     assert lines[1] == f"BS{which} = ["
-    assert len(lines) == 5
+    assert lines[-1] == f"]; %{title} [DOFs, elapsed, DOFs/s, BW (GB/s)]"
+    # three sizes (1, 2, 3 MiB of traffic); as in the reference, an entry below
+    # Nmax is followed by ";" even when it is the last one
+    assert sum(bool(re.fullmatch(ROW_VEC + ";?", ln)) for ln in lines) == 3
 
 
 @pytest.mark.gpu

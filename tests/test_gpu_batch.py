@@ -1,0 +1,72 @@
+"""Batched persistent launch and graph capture (GPU): every instance gets the same
+x, r and q bits as the one-instance entry points, and r.r within the reduction
+tolerance of the double-double oracle."""
+import numpy as np
+import pytest
+import torch
+
+from streamparanumal_gb300 import batch as B
+from streamparanumal_gb300 import kernels as K
+from streamparanumal_gb300 import ogs as O
+
+pytestmark = pytest.mark.gpu
+
+
+def instances(orc, count, seed, emax=5, pmax=5):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        ex, ey, ez = (int(v) for v in rng.integers(2, emax + 1, size=3))
+        p = int(rng.integers(2, pmax + 1))
+        ids = O.box_hex_ids(ex, ey, ez, p, int(rng.integers(0, 3)))
+        h = O.ogs_t()
+        h.Setup(ids.size, ids, unique=True)
+        n = ids.size
+        vec = {k: torch.from_numpy(orc.uniform(n, 100 * i + j)).cuda()
+               for j, k in enumerate(("x", "r", "p", "Ap", "q"))}
+        out.append((h, vec, 0.1 + 0.01 * i))
+    return out
+
+
+def test_batch_matches_single_instance_calls(cuda, orc):
+    inst = instances(orc, 7, 3)
+    ref = []
+    sc = K.ReduceScratch()
+    for h, v, alpha in inst:
+        x, r, q = v["x"].clone(), v["r"].clone(), v["q"].clone()
+        rr = torch.zeros(1, dtype=torch.float64, device="cuda")
+        K.cg_update(alpha, v["p"], v["Ap"], x, r, rr, sc)
+        h.GatherScatter(q, 1, O.Add, O.Sym)
+        xo, ro, rro = orc.cg_update(alpha, v["p"].cpu().numpy(), v["Ap"].cpu().numpy(),
+                                    v["x"].cpu().numpy(), v["r"].cpu().numpy())
+        ref.append((x, r, q, rro))
+    rdotr = [torch.zeros(1, dtype=torch.float64, device="cuda") for _ in inst]
+    b = B.Batch([h for h, _, _ in inst], [v["x"] for _, v, _ in inst],
+                [v["r"] for _, v, _ in inst], [v["p"] for _, v, _ in inst],
+                [v["Ap"] for _, v, _ in inst], rdotr, [v["q"] for _, v, _ in inst],
+                [a for _, _, a in inst])
+    b.run()
+    torch.cuda.synchronize()
+    for (h, v, _), (x, r, q, rro), rd in zip(inst, ref, rdotr):
+        assert torch.equal(v["x"], x) and torch.equal(v["r"], r) and torch.equal(v["q"], q)
+        assert abs(rd.item() - rro) <= 1e-14 * rro * 8
+
+
+def test_batch_graph_replay_and_repeat(cuda, orc):
+    inst = instances(orc, 4, 11)
+    rdotr = [torch.zeros(1, dtype=torch.float64, device="cuda") for _ in inst]
+    args = ([h for h, _, _ in inst], [v["x"] for _, v, _ in inst], [v["r"] for _, v, _ in inst],
+            [v["p"] for _, v, _ in inst], [v["Ap"] for _, v, _ in inst], rdotr,
+            [v["q"] for _, v, _ in inst], [0.0 for _ in inst])  # alpha 0: x, r unchanged
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        b = B.Batch(*args, stream=s)
+        b.run(stream=s)
+        first = [t.item() for t in rdotr]
+        g = B.Graph(s)
+        with g:
+            b.run(stream=s)
+        for _ in range(3):
+            g.launch()
+    torch.cuda.synchronize()
+    assert [t.item() for t in rdotr] == first  # tickets were reset; same order, same bits
