@@ -58,8 +58,8 @@ int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch
 int64_t     sp_launch_count(void);
 void        sp_launch_count_reset(void);
 /* Tuning knobs selecting among compiled kernel variants (process-wide; the
- * autotuner's surface).  Keys: "reduce.prefetch_chunks" (0..64, default 4): L2
- * bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
+ * autotuner's surface).  Keys: "reduce.prefetch_chunks" (-1..64, default -1 =
+ * per-kernel defaults): L2 bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
  * (256..2048, default 2048): non-zeros per row block of plans created afterwards;
  * "ogs.kernel" (0 block kernels, 1 warp-chunk kernels, 2 pipelined persistent
  * warp-chunk kernels; default 1); "ogs.order"

@@ -40,7 +40,7 @@ int sm_count();
 // ---------------------------------------------------------------- tuning knobs
 // Runtime-selectable launch parameters (the autotuner's surface, sp_tune_set/get).
 enum TuneKey : int {
-  kTuneReducePrefetch = 0,  // order-exact reductions: L2 bulk-prefetch distance in chunks (0 = off)
+  kTuneReducePrefetch = 0,  // order-exact reductions: L2 prefetch distance in chunks (-1 = per kernel)
   kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
   kTuneOgsKernel,           // ogs: 0 block, 1 warp-chunk, 2 pipelined persistent warp-chunk (k == 1)
   kTuneOgsOrder,            // ogs plan: warp-chunk order, 0 = rows, 1 = breadth-first pages

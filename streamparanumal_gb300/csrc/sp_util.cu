@@ -31,7 +31,7 @@ struct TuneEntry {
   std::atomic<int64_t> value;
 };
 static TuneEntry g_tune[kTuneCount] = {
-    {"reduce.prefetch_chunks", 0, 64, {4}},
+    {"reduce.prefetch_chunks", -1, 64, {-1}},
     {"ogs.block_nnz", 256, 2048, {2048}},
     {"ogs.kernel", 0, 2, {1}},
     {"ogs.order", 0, 1, {1}},

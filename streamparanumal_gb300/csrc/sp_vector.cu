@@ -436,20 +436,26 @@ static void launch_bs5_impl(int bs, int nb, int64_t n, const double* Ap, double 
   else if (bs == 512) k_bs5_1<512, 4, R><<<nb, 512, 0, s>>>(nb, n, Ap, alpha, r, part, pd);
   else k_bs5_1<1024, 4, R><<<nb, 1024, 0, s>>>(nb, n, Ap, alpha, r, part, pd);
 }
+// Prefetch distance: the knob when set (>= 0), else the per-kernel default measured
+// on GB300 with the rolling pipeline (BS3 0, BS4 16, BS5 0 chunks).
+static int prefetch_for(int dflt) {
+  const int64_t v = tune(kTuneReducePrefetch);
+  return v >= 0 ? (int)v : dflt;
+}
 static void launch_bs3(int bs, int nb, int64_t n, const double* a, double* part, cudaStream_t s) {
-  const int pd = (int)tune(kTuneReducePrefetch);
+  const int pd = prefetch_for(0);
   if (tune(kTuneReduceRolling)) launch_bs3_impl<true>(bs, nb, n, a, part, pd, s);
   else launch_bs3_impl<false>(bs, nb, n, a, part, pd, s);
 }
 static void launch_bs4(int bs, int nb, int64_t n, const double* a, const double* b, double* part,
                        cudaStream_t s) {
-  const int pd = (int)tune(kTuneReducePrefetch);
+  const int pd = prefetch_for(16);
   if (tune(kTuneReduceRolling)) launch_bs4_impl<true>(bs, nb, n, a, b, part, pd, s);
   else launch_bs4_impl<false>(bs, nb, n, a, b, part, pd, s);
 }
 static void launch_bs5(int bs, int nb, int64_t n, const double* Ap, double alpha, double* r,
                        double* part, cudaStream_t s) {
-  const int pd = (int)tune(kTuneReducePrefetch);
+  const int pd = prefetch_for(0);
   if (tune(kTuneReduceRolling)) launch_bs5_impl<true>(bs, nb, n, Ap, alpha, r, part, pd, s);
   else launch_bs5_impl<false>(bs, nb, n, Ap, alpha, r, part, pd, s);
 }
