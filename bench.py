@@ -50,6 +50,12 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="the batched workload: 256 uneven instances (CG update + BS8 each), "
                          "one persistent launch vs per-instance launches, plain and graphed")
+    ap.add_argument("--degree-sweep", default=None,
+                    help="comma list of degrees (e.g. 1-15): per degree, autotune and time "
+                         "BS6-BS8 on a box of ~1e8 local nodes, lexicographic and permuted")
+    ap.add_argument("--sweep-nodes", type=float, default=1e8)
+    ap.add_argument("--save-tuning", action="store_true",
+                    help="write the winners of --degree-sweep to the tuning table")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-emax", type=int, default=40)
     ap.add_argument("--kernels-only", action="store_true",
@@ -704,6 +710,68 @@ def run_batch(args, local_rank: int) -> None:
         Path(args.json_out).write_text(json.dumps(line, indent=1))
 
 
+def _degrees(spec: str) -> list[int]:
+    out = []
+    for part in spec.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            out += list(range(int(a), int(b) + 1))
+        else:
+            out.append(int(part))
+    return out
+
+
+def run_degree_sweep(args, local_rank: int) -> None:
+    """For each degree p the box edge is E = round((nodes / (p+1)^3)^(1/3)); the
+    autotuner times every ogs variant (FP64) and the winner is then timed in FP64
+    and FP32.  One JSON line per (p, layout)."""
+    import torch
+
+    from streamparanumal_gb300 import _build, autotune, capi
+    from streamparanumal_gb300 import ogs as O
+
+    _build.build_library()
+    capi.load()
+    torch.cuda.set_device(local_rank)
+    torch.manual_seed(args.seed)
+    peak, peak_kind = measured_peak()
+    table = autotune.load_table()
+    stream = torch.cuda.current_stream()
+    for p in _degrees(args.degree_sweep):
+        E = int(round((args.sweep_nodes / (p + 1) ** 3) ** (1.0 / 3.0)))
+        for perm in (0, args.perm_seed):
+            ids = O.box_hex_ids(E, E, E, p, perm)
+            res = autotune.tune_ogs(E, p, perm, ids=ids)
+            autotune.record(table, res)
+            best = res["best"]
+            autotune.apply(p, bool(perm), table)
+            h = O.ogs_t()
+            h.Setup(ids.size, ids, unique=True)
+            Nt, Ng = ids.size, h.NgatherGlobal
+            line = {"metric": "BS6-BS8 GB/s per degree (reference byte accounting)", "p": p,
+                    "E": E, "layout": "permuted" if perm else "lexicographic",
+                    "local_nodes": Nt, "global_nodes": Ng, "tuned": best, "peak": peak,
+                    "peak_source": peak_kind}
+            for dt, val in ((torch.float64, 8), (torch.float32, 4)):
+                q = (torch.rand(Nt, dtype=torch.float64, device="cuda") * 2 - 1).to(dt)
+                gq = torch.zeros(Ng, dtype=dt, device="cuda")
+                by = bytes_ogs(Nt, Ng, val)
+                by64 = bytes_ogs(Nt, Ng, 8)
+                t6 = _time(lambda: h.Gather(gq, q, 1, O.Add, O.Trans), stream, 10)
+                t7 = _time(lambda: h.Scatter(q, gq, 1, O.NoTrans), stream, 10)
+                t8 = _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), stream, 10)
+                key = "fp64" if val == 8 else "fp32"
+                line[key] = {k: {"ms": round(t, 4), "GBps": round(by[k] / 1e6 / t, 1),
+                                 "useful_GBps": round(by64[k] / 1e6 / t, 1),
+                                 "frac": round(by[k] / 1e6 / t / peak, 4)}
+                             for k, t in (("BS6", t6), ("BS7", t7), ("BS8", t8))}
+                del q, gq
+            h.Free()
+            print(json.dumps(line), flush=True)
+    if args.save_tuning:
+        autotune.save_table(table)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -715,6 +783,10 @@ def main():
     if args.batch:
         if rank == 0:
             run_batch(args, local_rank)
+        return
+    if args.degree_sweep:
+        if rank == 0:
+            run_degree_sweep(args, local_rank)
         return
     if world > 1:
         import torch

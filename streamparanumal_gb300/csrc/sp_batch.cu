@@ -119,8 +119,13 @@ k_batch(const BatchInst* __restrict__ inst, const BatchTask* __restrict__ tasks,
         __syncwarp();
         for (int32_t r = lane; r < nr; r += 32) {
           const int32_t a = srs[r], b = srs[r + 1];
+          // 0.0 + v0 == v0 except -0 -> +0: done as a 64-bit select, not an FP64 add
           double acc = 0.0;
-          for (int32_t i = a; i < b; ++i) acc = acc + sv[i];
+          if (a < b) {
+            const long long b0 = __double_as_longlong(sv[a]);
+            acc = __longlong_as_double(b0 == (long long)0x8000000000000000ULL ? 0LL : b0);
+          }
+          for (int32_t i = a + 1; i < b; ++i) acc = acc + sv[i];
           for (int32_t i = a; i < b; ++i) sv[i] = acc;
         }
         __syncwarp();

@@ -45,23 +45,59 @@ template <> __device__ __forceinline__ long long wrap_mul(long long a, long long
   return (long long)((unsigned long long)a * (unsigned long long)b);
 }
 
+// first(v) is apply(init(), v) computed without floating-point arithmetic where
+// that is exact: identity + v == v for every v except -0 (which becomes +0), and
+// 1 * v == v.  On GB300 the FP64 pipe is narrow, and this removes one FP64 add per
+// row -- every add of a multiplicity-1 row -- without changing a single bit.
+__device__ __forceinline__ double plus_zero(double v) {
+  const long long b = __double_as_longlong(v);
+  return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+__device__ __forceinline__ float plus_zero(float v) {
+  const int b = __float_as_int(v);
+  return __int_as_float(b == (int)0x80000000u ? 0 : b);
+}
+__device__ __forceinline__ int32_t plus_zero(int32_t v) { return v; }
+__device__ __forceinline__ long long plus_zero(long long v) { return v; }
+
 template <typename T, int OP> struct Op;
 template <typename T> struct Op<T, SP_OP_ADD> {
   static __device__ __forceinline__ T init() { return T(0); }
+  static __device__ __forceinline__ T first(T v) { return plus_zero(v); }
   static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_add(a, b); }
 };
 template <typename T> struct Op<T, SP_OP_MUL> {
   static __device__ __forceinline__ T init() { return T(1); }
+  static __device__ __forceinline__ T first(T v) { return v; }
   static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_mul(a, b); }
 };
 template <typename T> struct Op<T, SP_OP_MAX> {
   static __device__ __forceinline__ T init() { return -Lim<T>::big(); }
+  static __device__ __forceinline__ T first(T v) {
+    T a = init();
+    apply(a, v);
+    return a;
+  }
   static __device__ __forceinline__ void apply(T& a, T b) { a = (b > a) ? b : a; }
 };
 template <typename T> struct Op<T, SP_OP_MIN> {
   static __device__ __forceinline__ T init() { return Lim<T>::big(); }
+  static __device__ __forceinline__ T first(T v) {
+    T a = init();
+    apply(a, v);
+    return a;
+  }
   static __device__ __forceinline__ void apply(T& a, T b) { a = (b < a) ? b : a; }
 };
+
+// Combines s[a, b) in order from the op's identity.
+template <typename T, int OP>
+__device__ __forceinline__ T row_combine(const T* s, int32_t a, int32_t b) {
+  if (a >= b) return Op<T, OP>::init();
+  T acc = Op<T, OP>::first(s[a]);
+  for (int32_t i = a + 1; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
+  return acc;
+}
 
 // ------------------------------------------------------------------ kernels
 
@@ -105,8 +141,7 @@ k_ogs_gs_sym(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs,
   __syncthreads();
   for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
     const int32_t a = __ldg(rs + row) - g0, b = __ldg(rs + row + 1) - g0;
-    T acc = Op<T, OP>::init();
-    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
+    T acc = row_combine<T, OP>(s, a, b);
     for (int32_t i = a; i < b; ++i) s[i] = acc;
   }
   __syncthreads();
@@ -135,8 +170,7 @@ k_ogs_gs_gen(const int32_t* __restrict__ blocks, const int32_t* __restrict__ gS,
   __syncthreads();
   for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
     const int32_t a = __ldg(gS + row) - g0, b = __ldg(gS + row + 1) - g0;
-    T acc = Op<T, OP>::init();
-    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s_in[i]);
+    T acc = row_combine<T, OP>(s_in, a, b);
     const int32_t c = __ldg(sS + row) - s0, d = __ldg(sS + row + 1) - s0;
     for (int32_t i = c; i < d; ++i) s_out[i] = acc;
   }
@@ -161,8 +195,7 @@ k_ogs_gather(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs,
   __syncthreads();
   for (int32_t row = r0 + threadIdx.x; row < r1; row += kOgsThreads) {
     const int32_t a = __ldg(rs + row) - g0, b = __ldg(rs + row + 1) - g0;
-    T acc = Op<T, OP>::init();
-    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
+    T acc = row_combine<T, OP>(s, a, b);
     gv[k + (int64_t)row * K] = acc;
   }
 }
@@ -246,8 +279,7 @@ k_ogsw_gs_sym(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
     const int32_t a = srs[r], b = srs[r + 1];
-    T acc = Op<T, OP>::init();
-    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+    T acc = row_combine<T, OP>(sv, a, b);
     for (int32_t i = a; i < b; ++i) sv[i] = acc;
   }
   __syncwarp();
@@ -275,8 +307,7 @@ k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
     const int32_t a = srs[r], b = srs[r + 1];
-    T acc = Op<T, OP>::init();
-    for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+    T acc = row_combine<T, OP>(sv, a, b);
     gv[ch.x + r] = acc;
   }
 }
@@ -356,8 +387,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
     __syncwarp();
     for (int32_t r = lane; r < nr; r += 32) {
       const int32_t a = srs[r], b = srs[r + 1];
-      T acc = Op<T, OP>::init();
-      for (int32_t i = a; i < b; ++i) Op<T, OP>::apply(acc, sv[i]);
+      T acc = row_combine<T, OP>(sv, a, b);
       if (MODE == 0) {
         for (int32_t i = a; i < b; ++i) sv[i] = acc;
       } else {

@@ -66,13 +66,13 @@ def test_bs1_to_bs5_rows(cuda, bsdir, which, title, extra):
                         r"\(GB/s\)\]\n", out), out
     out = run(bsdir, f"BS{which}", "-bmin", 1 << 20, "-bmax", 3 << 20, "-s", 1 << 20,
               *extra).stdout
-    lines = out.strip().split("\n")
-    assert lines[0] == f"%{title} [DOFs, elapsed, DOFs/s, BW (GB/s)]"
-    assert lines[1] == f"BS{which} = ["
-    assert lines[-1] == f"]; %{title} [DOFs, elapsed, DOFs/s, BW (GB/s)]"
-    # three sizes (1, 2, 3 MiB of traffic); as in the reference, an entry below
-    # Nmax is followed by ";" even when it is the last one
-    assert sum(bool(re.fullmatch(ROW_VEC + ";?", ln)) for ln in lines) == 3
+    # sweep block: header, "BSx = [", entries separated by ";\n", and "]; %title [...]"
+    # right after the last entry (bs1Run.cpp:86-90: ";" only while N < Nmax)
+    m = re.fullmatch(rf"%{title} \[DOFs, elapsed, DOFs/s, BW \(GB/s\)\]\nBS{which} = \[\n"
+                     rf"((?:{ROW_VEC};\n)*{ROW_VEC};?\n?)\]; %{title} \[DOFs, elapsed, DOFs/s, "
+                     r"BW \(GB/s\)\]\n", out)
+    assert m, out
+    assert len(re.findall(ROW_VEC, m.group(1))) == 3
 
 
 @pytest.mark.gpu
