@@ -51,6 +51,7 @@ struct Groups {
 static void build_groups(int32_t N, const int64_t* ids, Groups& g) {
   int64_t maxAbs = 0;
   int32_t nids = 0;
+#pragma omp parallel for schedule(static) reduction(max : maxAbs) reduction(+ : nids)
   for (int32_t l = 0; l < N; ++l)
     if (ids[l] != 0) {
       maxAbs = std::max(maxAbs, iabs64(ids[l]));
@@ -61,18 +62,37 @@ static void build_groups(int32_t N, const int64_t* ids, Groups& g) {
   if (nids == 0) return;
   const int64_t directLimit = std::max<int64_t>(4 * (int64_t)N, 1 << 20);
   if (maxAbs <= directLimit) {
-    // counting sort by key: O(N + maxAbs)
-    std::vector<int32_t> cnt((size_t)maxAbs + 2, 0);
+    // counting sort by key, in parallel: histogram, scan, atomic placement, then
+    // each group's members sorted (groups are small), so the result is the stable
+    // order whatever the thread schedule
+    const size_t nkeys = (size_t)maxAbs + 2;
+    std::vector<int32_t> cnt(nkeys, 0);
+#pragma omp parallel for schedule(static)
     for (int32_t l = 0; l < N; ++l)
-      if (ids[l] != 0) ++cnt[(size_t)iabs64(ids[l]) + 1];
-    std::vector<int32_t> keyGroup;  // not needed beyond offsets
-    for (size_t k = 1; k < cnt.size(); ++k) cnt[k] += cnt[k - 1];
+      if (ids[l] != 0) {
+#pragma omp atomic
+        ++cnt[(size_t)iabs64(ids[l]) + 1];
+      }
+    std::vector<int32_t> fill(nkeys, 0);
+    int32_t running = 0;
+    for (size_t k = 1; k < nkeys; ++k) {
+      if (cnt[k] != 0) g.offsets.push_back(running + cnt[k]);
+      running += cnt[k];
+      fill[k - 1] = running - cnt[k];  // start of key k-1's bucket
+    }
     g.members.resize(nids);
-    std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+#pragma omp parallel for schedule(static)
     for (int32_t l = 0; l < N; ++l)
-      if (ids[l] != 0) g.members[fill[(size_t)iabs64(ids[l])]++] = l;
-    for (size_t k = 1; k < cnt.size(); ++k)
-      if (cnt[k] != cnt[k - 1]) g.offsets.push_back(cnt[k]);
+      if (ids[l] != 0) {
+        int32_t pos;
+#pragma omp atomic capture
+        pos = fill[(size_t)iabs64(ids[l])]++;
+        g.members[pos] = l;
+      }
+    const int32_t ng = (int32_t)g.offsets.size() - 1;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int32_t n = 0; n < ng; ++n)
+      std::sort(g.members.begin() + g.offsets[n], g.members.begin() + g.offsets[n + 1]);
   } else {
     std::vector<std::pair<int64_t, int32_t>> kv;
     kv.reserve(nids);
@@ -110,10 +130,15 @@ sp_status sp_ogs_setup_csr(int32_t N, int64_t* ids, sp_kind kind, int32_t unique
   const int32_t ngroups = (int32_t)g.offsets.size() - 1;
 
   if (unique) {
+    // the draws follow the groups in ascending |id| (one sequential LCG pass), the
+    // sign writes are independent per group
+    std::vector<int32_t> draw(ngroups);
     Lcg rng(0);  // seedRNG(rank) with rank 0
+    for (int32_t n = 0; n < ngroups; ++n) draw[n] = rng.next_int();
+#pragma omp parallel for schedule(static)
     for (int32_t n = 0; n < ngroups; ++n) {
       const int32_t a = g.offsets[n], b = g.offsets[n + 1];
-      const int32_t m = rng.next_int() % (b - a);
+      const int32_t m = draw[n] % (b - a);
       const int64_t key = iabs64(ids[g.members[a]]);
       for (int32_t i = a; i < b; ++i) ids[g.members[i]] = -key;
       if (m >= 0) ids[g.members[a + m]] = key;
@@ -122,19 +147,27 @@ sp_status sp_ogs_setup_csr(int32_t N, int64_t* ids, sp_kind kind, int32_t unique
 
   // group sign; members ascend, so members[offsets[n]] is the first appearance
   std::vector<uint8_t> positive(ngroups, 0);
-  for (int32_t n = 0; n < ngroups; ++n)
+  std::vector<int32_t> firstOf(N > 0 ? N : 1, -1);
+#pragma omp parallel for schedule(static)
+  for (int32_t n = 0; n < ngroups; ++n) {
     for (int32_t i = g.offsets[n]; i < g.offsets[n + 1]; ++i)
       if (ids[g.members[i]] > 0) {
         positive[n] = 1;
         break;
       }
-  // rows: positive groups by first appearance, then the flagged-only groups
-  std::vector<int32_t> order(ngroups);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-    if (positive[x] != positive[y]) return positive[x] > positive[y];
-    return g.members[g.offsets[x]] < g.members[g.offsets[y]];
-  });
+    firstOf[g.members[g.offsets[n]]] = n;
+  }
+  // rows: positive groups by first appearance, then the flagged-only groups.  A
+  // group's first member is its smallest local index, so scanning local indices in
+  // ascending order meets the groups in first-appearance order (linear time).
+  std::vector<int32_t> order;
+  order.reserve(ngroups);
+  for (int pass = 1; pass >= 0; --pass)
+    for (int32_t l = 0; l < N; ++l) {
+      const int32_t n = firstOf[l];
+      if (n >= 0 && positive[n] == pass) order.push_back(n);
+    }
+  std::vector<int32_t>().swap(firstOf);
   int32_t NrowsP = 0;
   for (int32_t n = 0; n < ngroups; ++n) NrowsP += positive[n];
 
@@ -142,18 +175,31 @@ sp_status sp_ogs_setup_csr(int32_t N, int64_t* ids, sp_kind kind, int32_t unique
   rowStartsT[0] = 0;
   for (int32_t r = 0; r < ngroups; ++r) {
     const int32_t n = order[r];
-    const int32_t a = g.offsets[n], b = g.offsets[n + 1];
-    std::copy(g.members.begin() + a, g.members.begin() + b, colIdsT + rowStartsT[r]);
-    rowStartsT[r + 1] = rowStartsT[r] + (b - a);
+    rowStartsT[r + 1] = rowStartsT[r] + (g.offsets[n + 1] - g.offsets[n]);
+  }
+#pragma omp parallel for schedule(static)
+  for (int32_t r = 0; r < ngroups; ++r) {
+    const int32_t n = order[r];
+    std::copy(g.members.begin() + g.offsets[n], g.members.begin() + g.offsets[n + 1],
+              colIdsT + rowStartsT[r]);
   }
   // N operator: positive members (Signed, Halo) or every member (Unsigned)
   *NrowsN = NrowsP;
-  rowStartsN[0] = 0;
-  int32_t nn = 0;
+  std::vector<int32_t> cntN(NrowsP + 1, 0);
+#pragma omp parallel for schedule(static)
   for (int32_t r = 0; r < NrowsP; ++r) {
+    int32_t c = 0;
+    for (int32_t i = rowStartsT[r]; i < rowStartsT[r + 1]; ++i)
+      c += (kind == SP_KIND_UNSIGNED || ids[colIdsT[i]] > 0) ? 1 : 0;
+    cntN[r] = c;
+  }
+  rowStartsN[0] = 0;
+  for (int32_t r = 0; r < NrowsP; ++r) rowStartsN[r + 1] = rowStartsN[r] + cntN[r];
+#pragma omp parallel for schedule(static)
+  for (int32_t r = 0; r < NrowsP; ++r) {
+    int32_t nn = rowStartsN[r];
     for (int32_t i = rowStartsT[r]; i < rowStartsT[r + 1]; ++i)
       if (kind == SP_KIND_UNSIGNED || ids[colIdsT[i]] > 0) colIdsN[nn++] = colIdsT[i];
-    rowStartsN[r + 1] = nn;
   }
   return SP_SUCCESS;
 }
