@@ -61,8 +61,9 @@ void        sp_launch_count_reset(void);
  * autotuner's surface).  Keys: "reduce.prefetch_chunks" (-1..64, default -1 =
  * per-kernel defaults): L2 bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
  * (256..2048, default 2048): non-zeros per row block of plans created afterwards;
- * "ogs.kernel" (0 block kernels, 1 warp-chunk kernels, 2 pipelined persistent
- * warp-chunk kernels; default 1); "ogs.order"
+ * "ogs.kernel" / "ogs.kernel.gather" /
+ * "ogs.kernel.scatter" (gather+scatter / gather / scatter: 0 block kernels, 1
+ * warp-chunk kernels, 2 pipelined persistent warp-chunk kernels; defaults 2, 2, 1); "ogs.order"
  * (0 row order, 1 breadth-first over 4 KiB pages; default 1) for the warp chunks of
  * plans created afterwards; "reduce.rolling" (1 rolling load pipeline, 0 grouped
  * loads; default 1) for the order-exact reductions.

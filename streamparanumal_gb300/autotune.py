@@ -41,46 +41,63 @@ def _time(fn, reps: int, stream) -> float:
     return e0.elapsed_time(e1) / reps
 
 
+KNOBS = {"order": "ogs.order", "block_nnz": "ogs.block_nnz", "kernel_gs": "ogs.kernel",
+         "kernel_gather": "ogs.kernel.gather", "kernel_scatter": "ogs.kernel.scatter"}
+
+
 def _set(cfg: dict) -> None:
-    capi.tune_set("ogs.order", cfg["order"])
-    capi.tune_set("ogs.block_nnz", cfg["block_nnz"])
-    capi.tune_set("ogs.kernel", cfg["kernel"])
+    for k, knob in KNOBS.items():
+        if k in cfg:
+            capi.tune_set(knob, cfg[k])
 
 
 def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
              ids=None) -> dict:
-    """Times every variant on an E^3 box of degree p; returns the winner and all
-    timings (ms per call)."""
-    saved = {k: capi.tune_get(f"ogs.{k}") for k in ("order", "block_nnz", "kernel")}
+    """Times every variant of BS6 / BS7 / BS8 on an E^3 box of degree p; the winner
+    takes, for the best chunk order, the fastest kernel of each operation."""
+    saved = {k: capi.tune_get(knob) for k, knob in KNOBS.items()}
     stream = torch.cuda.current_stream()
     if ids is None:
         ids = O.box_hex_ids(E, E, E, p, perm_seed)
     Nt = ids.size
     q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
-    results = []
+    timings = []  # (order, block_nnz, kernel, op, ms)
     try:
         for pc in PLAN_CONFIGS:
-            _set({**pc, "kernel": 1})
+            _set(pc)
             h = O.ogs_t()
             h.Setup(Nt, ids.copy(), unique=True)
             gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
             kernels = [0] if pc["order"] == 0 else []
             kernels += [1, 2] if pc["block_nnz"] == 2048 else []
             for k in kernels:
-                capi.tune_set("ogs.kernel", k)
-                t6 = _time(lambda: h.Gather(gq, q, 1, O.Add, O.Trans), reps, stream)
-                t7 = _time(lambda: h.Scatter(q, gq, 1, O.NoTrans), reps, stream)
-                t8 = _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), reps, stream)
-                results.append({**pc, "kernel": k, "ms": {"BS6": t6, "BS7": t7, "BS8": t8},
-                                "total_ms": t6 + t7 + t8})
+                _set({"kernel_gs": k, "kernel_gather": k, "kernel_scatter": k})
+                ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
+                       "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
+                       "BS8": lambda: h.GatherScatter(q, 1, O.Add, O.Sym)}
+                for op, fn in ops.items():
+                    timings.append((pc["order"], pc["block_nnz"], k, op, _time(fn, reps, stream)))
             h.Free()
             del gq
     finally:
         _set(saved)
-    best = min(results, key=lambda r: r["total_ms"])
-    return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt),
-            "best": {k: best[k] for k in ("kernel", "order", "block_nnz")},
-            "candidates": results}
+    best_total, best = None, None
+    for order in sorted({t[0] for t in timings}):
+        choice, total = {"order": order}, 0.0
+        for op, key in (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs")):
+            cands = [t for t in timings if t[3] == op and (t[0] == order or t[2] == 0)]
+            o, bnnz, k, _, ms = min(cands, key=lambda t: t[4])
+            choice[key] = k
+            if k == 0:
+                choice["block_nnz"] = bnnz
+            total += ms
+        if best_total is None or total < best_total:
+            best_total, best = total, choice
+    best.setdefault("block_nnz", 2048)
+    return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,
+            "best_total_ms": best_total,
+            "candidates": [{"order": o, "block_nnz": b, "kernel": k, "op": op, "ms": ms}
+                           for o, b, k, op, ms in timings]}
 
 
 def load_table(path: Path = TABLE) -> dict:

@@ -459,11 +459,11 @@ static inline unsigned warp_grid(int32_t nchunks) {
   return (unsigned)((nchunks + kWarpsPerCta - 1) / kWarpsPerCta);
 }
 
-static inline bool use_warp(const sp_ogs_plan* p, int K, int32_t nchunks) {
-  return K == 1 && nchunks > 0 && tune(kTuneOgsKernel) == 1;
-}
-static inline bool use_pipe(const sp_ogs_plan* p, int K, int32_t nchunks) {
-  return K == 1 && nchunks > 0 && tune(kTuneOgsKernel) == 2;
+// Kernel variant of an operation (knobs ogs.kernel / ogs.kernel.gather /
+// ogs.kernel.scatter): 0 block kernels, 1 warp chunks, 2 pipelined warp chunks.
+// The warp variants need k == 1 and a plan with chunks.
+static inline int variant(TuneKey key, int K, int32_t nchunks) {
+  return (K == 1 && nchunks > 0) ? (int)tune(key) : 0;
 }
 
 // ------------------------------------------------------------------ dispatch
@@ -472,11 +472,11 @@ template <typename T, int OP>
 static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
-  if ((trans == SP_SYM || p->n_is_t) && use_pipe(p, K, p->nchunksT)) {
+  if ((trans == SP_SYM || p->n_is_t) && variant(kTuneOgsKernel, K, p->nchunksT) == 2) {
     k_ogsp_gather<T, OP, 0><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         v, nullptr);
-  } else if ((trans == SP_SYM || p->n_is_t) && use_warp(p, K, p->nchunksT)) {
+  } else if ((trans == SP_SYM || p->n_is_t) && variant(kTuneOgsKernel, K, p->nchunksT) == 1) {
     k_ogsw_gs_sym<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT, v);
   } else if (trans == SP_SYM || p->n_is_t) {
@@ -495,19 +495,19 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
 template <typename T, int OP>
 static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
                           cudaStream_t s) {
-  if (trans == SP_NOTRANS && use_pipe(p, K, p->nchunksN)) {
+  if (trans == SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksN) == 2) {
     k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, const_cast<T*>(v), gv);
-  } else if (trans != SP_NOTRANS && use_pipe(p, K, p->nchunksT)) {
+  } else if (trans != SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksT) == 2) {
     k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         const_cast<T*>(v), gv);
-  } else if (trans == SP_NOTRANS && use_warp(p, K, p->nchunksN)) {
+  } else if (trans == SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksN) == 1) {
     k_ogsw_gather<T, OP><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, v, gv);
-  } else if (trans != SP_NOTRANS && use_warp(p, K, p->nchunksT)) {
+  } else if (trans != SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksT) == 1) {
     k_ogsw_gather<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         v, gv);
@@ -525,19 +525,19 @@ static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv
 template <typename T>
 static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, const T* gv,
                            cudaStream_t s) {
-  if (trans == SP_TRANS && use_pipe(p, K, p->nchunksN)) {
+  if (trans == SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksN) == 2) {
     k_ogsp_scatter<T><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, gv, v);
-  } else if (trans != SP_TRANS && use_pipe(p, K, p->nchunksT)) {
+  } else if (trans != SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksT) == 2) {
     k_ogsp_scatter<T><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         gv, v);
-  } else if (trans == SP_TRANS && use_warp(p, K, p->nchunksN)) {
+  } else if (trans == SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksN) == 1) {
     k_ogsw_scatter<T><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
         p->d_colIdsN, gv, v);
-  } else if (trans != SP_TRANS && use_warp(p, K, p->nchunksT)) {
+  } else if (trans != SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksT) == 1) {
     k_ogsw_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
         gv, v);

@@ -1,0 +1,38 @@
+"""The autotuner times every ogs variant and its winner reproduces the reference's
+bits (GPU)."""
+import numpy as np
+import pytest
+import torch
+
+from streamparanumal_gb300 import autotune, capi
+from streamparanumal_gb300 import ogs as O
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tune_and_apply_small_box(cuda, orc, tmp_path):
+    saved = {k: capi.tune_get(v) for k, v in autotune.KNOBS.items()}
+    try:
+        res = autotune.tune_ogs(4, 3, perm_seed=5, reps=2)
+        best = res["best"]
+        assert set(best) >= {"order", "kernel_gs", "kernel_gather", "kernel_scatter", "block_nnz"}
+        assert len(res["candidates"]) == 15  # 5 (plan, kernel) pairs x 3 operations
+        table = {}
+        autotune.record(table, res)
+        path = tmp_path / "t.json"
+        autotune.save_table(table, path)
+        cfg = autotune.apply(3, True, autotune.load_table(path))
+        assert cfg == best
+        ids = O.box_hex_ids(4, 4, 4, 3, 5)
+        ref = orc.ogs_setup(ids.copy(), kind=1, unique=True)
+        h = O.ogs_t()
+        h.Setup(ids.size, ids, unique=True)
+        q = orc.uniform(ids.size, 4)
+        dq = torch.from_numpy(q).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(
+            dq.cpu().numpy(),
+            orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], q))
+    finally:
+        autotune._set(saved)

@@ -188,9 +188,11 @@ def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
     """Block kernels, and warp-chunk kernels in row and breadth-first order, all give
     the reference's bits (each row is still summed by one lane in CSR order)."""
     nx, ny, nz, p, seed = box
-    old = (capi.tune_get("ogs.kernel"), capi.tune_get("ogs.order"))
+    keys = ("ogs.kernel", "ogs.kernel.gather", "ogs.kernel.scatter", "ogs.order")
+    old = {k: capi.tune_get(k) for k in keys}
     try:
-        capi.tune_set("ogs.kernel", kernel)
+        for k in keys[:3]:
+            capi.tune_set(k, kernel)
         capi.tune_set("ogs.order", order)
         ids = O.box_hex_ids(nx, ny, nz, p, seed)
         h, ref = make(orc, ids)
@@ -211,5 +213,5 @@ def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
         h.Gather(gN, torch.from_numpy(q).cuda(), 1, O.Add, O.NoTrans)
         np.testing.assert_array_equal(host(gN), orc.gather(ref["rsN"], ref["ciN"], q))
     finally:
-        capi.tune_set("ogs.kernel", old[0])
-        capi.tune_set("ogs.order", old[1])
+        for k, v in old.items():
+            capi.tune_set(k, v)
