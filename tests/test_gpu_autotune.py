@@ -16,7 +16,7 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
         res = autotune.tune_ogs(4, 3, perm_seed=5, reps=2)
         best = res["best"]
         assert set(best) >= {"order", "kernel_gs", "kernel_gather", "kernel_scatter", "block_nnz"}
-        assert len(res["candidates"]) == 15  # 5 (plan, kernel) pairs x 3 operations
+        assert len(res["candidates"]) == 18  # 6 (plan, kernel) pairs x 3 operations
         table = {}
         autotune.record(table, res)
         path = tmp_path / "t.json"
