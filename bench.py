@@ -393,16 +393,45 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     h_scal = torch.empty(4, dtype=torch.float64).pin_memory()
     e2e_steps = max(3, min(args.steps, 20))
 
+    # copies on their own streams so that they overlap the kernels of the same step:
+    # q uploads while BS1-BS5 run, r (= b after BS5) downloads while BS6-BS8 run
+    s_in = torch.cuda.Stream(device=dev)
+    s_out = torch.cuda.Stream(device=dev)
+
     def e2e_step():
-        with torch.cuda.stream(stream):
+        ev_start = torch.cuda.Event()
+        ev_start.record(stream)
+        s_in.wait_event(ev_start)           # previous step's kernels are done with a, b, q
+        with torch.cuda.stream(s_in):
             a.copy_(h_a, non_blocking=True)
             b.copy_(h_b, non_blocking=True)
+            ev_ab = torch.cuda.Event()
+            ev_ab.record(s_in)
             q.copy_(h_q, non_blocking=True)
-            for _ in suite():
-                pass
+            ev_q = torch.cuda.Event()
+            ev_q.record(s_in)
+        stream.wait_event(ev_ab)
+        it = suite()
+        for name in it:                   # BS1 ... BS5
+            if name == "BS5":
+                break
+        ev_bs5 = torch.cuda.Event()
+        ev_bs5.record(stream)
+        s_out.wait_event(ev_bs5)
+        with torch.cuda.stream(s_out):
             h_out_b.copy_(b, non_blocking=True)
+        stream.wait_event(ev_q)
+        for _ in it:                      # BS6 ... BS8
+            pass
+        ev_end = torch.cuda.Event()
+        ev_end.record(stream)
+        s_out.wait_event(ev_end)
+        with torch.cuda.stream(s_out):
             h_out_q.copy_(q, non_blocking=True)
             h_scal.copy_(scal, non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(s_out)
+        stream.wait_event(done)           # the step ends when its results are on the host
 
     for _ in range(2):
         e2e_step()
