@@ -77,6 +77,25 @@ def bytes_ogs(Nt: int, Ng: int, val: int = 8) -> dict:
             "BS8": (Ng + 1) * 4 + Nt * 4 + 2 * Nt * val}
 
 
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over all ranks of the process group (the job's step time is its
+    slowest replica's); x itself when no group is running."""
+    import torch
+    import torch.distributed as tdist
+
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, bytes_per_step: int, ms_per_step: float) -> float:
+    """Whole-job GB/s: every replica moves bytes_per_step per step (weak scaling)."""
+    return world * bytes_per_step / 1e9 / (ms_per_step / 1e3)
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -374,12 +393,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         for i, n in enumerate(names):
             per[n] += ev[i].elapsed_time(ev[i + 1])
     per = {n: v / args.steps for n, v in per.items()}  # ms per call
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
-    value = world * step_bytes / 1e9 / (ms_per_step / 1e3)
+    value = job_rate(world, step_bytes, ms_per_step)
 
     if args.kernels_only:
         if rank == 0:
@@ -445,14 +461,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, dev)
     h2d = (h_a.numel() + h_b.numel() + h_q.numel()) * 8
     d2h = (h_out_b.numel() + h_out_q.numel() + h_scal.numel()) * 8
-    e2e_value = world * step_bytes / 1e9 / (e2e_ms / 1e3)
+    e2e_value = job_rate(world, step_bytes, e2e_ms)
 
     # ---- BS0 launch latency: 10,000 empty launches, plain and graph-captured
     bs0 = bs0_latency(stream, dev)
