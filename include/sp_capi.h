@@ -58,15 +58,20 @@ int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch
 int64_t     sp_launch_count(void);
 void        sp_launch_count_reset(void);
 /* Tuning knobs selecting among compiled kernel variants (process-wide; the
- * autotuner's surface).  Keys: "reduce.prefetch_chunks" (-1..64, default -1 =
- * per-kernel defaults): L2 bulk-prefetch distance of the order-exact reductions; "ogs.block_nnz"
- * (256..2048, default 2048): non-zeros per row block of plans created afterwards;
- * "ogs.kernel" / "ogs.kernel.gather" /
- * "ogs.kernel.scatter" (gather+scatter / gather / scatter: 0 block kernels, 1
- * warp-chunk kernels, 2 pipelined persistent warp-chunk kernels; defaults 2, 2, 1); "ogs.order"
- * (0 row order, 1 breadth-first over 4 KiB pages; default 1) for the warp chunks of
- * plans created afterwards; "reduce.rolling" (1 rolling load pipeline, 0 grouped
- * loads; default 1) for the order-exact reductions.
+ * autotuner's surface).  Every variant computes the same bits.  Keys:
+ *  "reduce.prefetch_chunks" (-1..64, default -1 = per-kernel defaults): L2
+ *    bulk-prefetch distance of the order-exact reductions;
+ *  "reduce.rolling" (1 rolling load pipeline, 0 grouped loads; default 1) for the
+ *    order-exact reductions;
+ *  "ogs.block_nnz" (256..2048, default 2048): non-zeros per row block of plans
+ *    created afterwards;
+ *  "ogs.order" (0 row order, 1 breadth-first over 4 KiB pages; default 1) and
+ *    "ogs.rows" (0 CSR order, 1 rows grouped by size inside a chunk; default 1) for
+ *    the warp chunks of plans created afterwards;
+ *  "ogs.kernel" / "ogs.kernel.gather" / "ogs.kernel.scatter" (gather+scatter /
+ *    gather / scatter): 0 block kernels, 1 warp-chunk kernels, 2 pipelined
+ *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
+ *    the column-order scatter, 4 column-order pipelined gathers; defaults 2, 2, 3.
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);
@@ -197,7 +202,7 @@ typedef struct {
   int32_t NchunksT;   /* warp chunks of the T / N operators (0: block kernels only) */
   int32_t NchunksN;
   int32_t chunkOrder; /* 0 row order, 1 breadth-first over 4 KiB pages             */
-  int32_t reserved;
+  int32_t rowOrder;   /* T rows inside a chunk: 0 CSR order, 1 grouped by size      */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

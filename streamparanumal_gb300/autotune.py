@@ -2,9 +2,10 @@
 
 For a hex box of degree p it times BS6 (Gather Trans), BS7 (Scatter NoTrans) and
 BS8 (GatherScatter Sym) under every compiled variant -- block kernels (rows cut into
-blocks of `ogs.block_nnz` entries), warp-chunk kernels and pipelined persistent
-warp-chunk kernels, each with chunks in row order or breadth-first page order --
-and keeps the fastest by total time.  Results are stored per degree in a JSON table
+blocks of `ogs.block_nnz` entries), warp-chunk kernels, pipelined persistent
+warp-chunk kernels and asynchronously staged ones, each with chunks in row order or
+breadth-first page order and rows in CSR order or grouped by size -- and keeps the
+fastest by total time.  Results are stored per degree in a JSON table
 (`tuning/gb300.json` by default) that :func:`apply` loads into the library's tuning
 knobs before plans are built.  Every variant computes the same bits; only speed
 differs.
@@ -21,11 +22,14 @@ from . import ogs as O
 
 TABLE = Path(__file__).resolve().parent / "tuning" / "gb300.json"
 
-# (plan-time knobs) x (launch-time kernel): plans are rebuilt only when order or
-# block_nnz change
-PLAN_CONFIGS = [{"order": 1, "block_nnz": 2048}, {"order": 0, "block_nnz": 2048},
-                {"order": 0, "block_nnz": 1024}]
-KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined"}
+# (plan-time knobs) x (launch-time kernel): plans are rebuilt only when order, rows
+# or block_nnz change
+PLAN_CONFIGS = [{"order": 1, "rows": 1, "block_nnz": 2048}, {"order": 1, "rows": 0, "block_nnz": 2048},
+                {"order": 0, "rows": 1, "block_nnz": 2048}, {"order": 0, "rows": 0, "block_nnz": 2048},
+                {"order": 0, "rows": 0, "block_nnz": 1024}]
+KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
+           3: "warp-async-staged gathers / column-order scatter", 4: "column-order gathers"}
+OPS = (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs"))
 
 
 def _time(fn, reps: int, stream) -> float:
@@ -41,8 +45,9 @@ def _time(fn, reps: int, stream) -> float:
     return e0.elapsed_time(e1) / reps
 
 
-KNOBS = {"order": "ogs.order", "block_nnz": "ogs.block_nnz", "kernel_gs": "ogs.kernel",
-         "kernel_gather": "ogs.kernel.gather", "kernel_scatter": "ogs.kernel.scatter"}
+KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "block_nnz": "ogs.block_nnz",
+         "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
+         "kernel_scatter": "ogs.kernel.scatter"}
 
 
 def _set(cfg: dict) -> None:
@@ -51,42 +56,56 @@ def _set(cfg: dict) -> None:
             capi.tune_set(knob, cfg[k])
 
 
+def _kernels(pc: dict, op: str) -> list[int]:
+    """Kernel variants timed under one plan configuration: block kernels ignore the
+    chunk order and row grouping, so they run once per block size; the column-order
+    scatter ignores the row grouping, so it runs under grouped plans only."""
+    ks = [0] if (pc["order"] == 0 and pc["rows"] == 0) else []
+    if pc["block_nnz"] == 2048:
+        if op == "BS7":
+            ks += [1, 2] + ([3] if pc["rows"] == 1 else [])
+        else:
+            ks += [1, 2, 3, 4]
+    return ks
+
+
 def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
              ids=None) -> dict:
     """Times every variant of BS6 / BS7 / BS8 on an E^3 box of degree p; the winner
-    takes, for the best chunk order, the fastest kernel of each operation."""
+    takes, for the best (chunk order, row grouping), the fastest kernel of each
+    operation."""
     saved = {k: capi.tune_get(knob) for k, knob in KNOBS.items()}
     stream = torch.cuda.current_stream()
     if ids is None:
         ids = O.box_hex_ids(E, E, E, p, perm_seed)
     Nt = ids.size
     q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
-    timings = []  # (order, block_nnz, kernel, op, ms)
+    timings = []  # (order, rows, block_nnz, kernel, op, ms)
     try:
         for pc in PLAN_CONFIGS:
             _set(pc)
             h = O.ogs_t()
             h.Setup(Nt, ids.copy(), unique=True)
             gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
-            kernels = [0] if pc["order"] == 0 else []
-            kernels += [1, 2] if pc["block_nnz"] == 2048 else []
-            for k in kernels:
-                _set({"kernel_gs": k, "kernel_gather": k, "kernel_scatter": k})
-                ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
-                       "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
-                       "BS8": lambda: h.GatherScatter(q, 1, O.Add, O.Sym)}
-                for op, fn in ops.items():
-                    timings.append((pc["order"], pc["block_nnz"], k, op, _time(fn, reps, stream)))
+            ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
+                   "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
+                   "BS8": lambda: h.GatherScatter(q, 1, O.Add, O.Sym)}
+            for op, key in OPS:
+                for k in _kernels(pc, op):
+                    _set({key: k})
+                    timings.append((pc["order"], pc["rows"], pc["block_nnz"], k, op,
+                                    _time(ops[op], reps, stream)))
             h.Free()
             del gq
     finally:
         _set(saved)
     best_total, best = None, None
-    for order in sorted({t[0] for t in timings}):
-        choice, total = {"order": order}, 0.0
-        for op, key in (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs")):
-            cands = [t for t in timings if t[3] == op and (t[0] == order or t[2] == 0)]
-            o, bnnz, k, _, ms = min(cands, key=lambda t: t[4])
+    for order, rows in sorted({(t[0], t[1]) for t in timings}):
+        choice, total = {"order": order, "rows": rows}, 0.0
+        for op, key in OPS:
+            cands = [t for t in timings
+                     if t[4] == op and ((t[0], t[1]) == (order, rows) or t[3] == 0)]
+            _, _, bnnz, k, _, ms = min(cands, key=lambda t: t[5])
             choice[key] = k
             if k == 0:
                 choice["block_nnz"] = bnnz
@@ -96,8 +115,8 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
     best.setdefault("block_nnz", 2048)
     return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,
             "best_total_ms": best_total,
-            "candidates": [{"order": o, "block_nnz": b, "kernel": k, "op": op, "ms": ms}
-                           for o, b, k, op, ms in timings]}
+            "candidates": [{"order": o, "rows": r, "block_nnz": b, "kernel": k, "op": op, "ms": ms}
+                           for o, r, b, k, op, ms in timings]}
 
 
 def load_table(path: Path = TABLE) -> dict:

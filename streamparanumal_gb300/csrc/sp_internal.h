@@ -42,11 +42,12 @@ int sm_count();
 enum TuneKey : int {
   kTuneReducePrefetch = 0,  // order-exact reductions: L2 prefetch distance in chunks (-1 = per kernel)
   kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
-  kTuneOgsKernel,           // ogs gather+scatter: 0 block, 1 warp-chunk, 2 pipelined warp-chunk (k == 1)
+  kTuneOgsKernel,           // ogs gather+scatter: 0 block, 1 warp-chunk, 2 pipelined, 3 async-staged (k == 1)
   kTuneOgsOrder,            // ogs plan: warp-chunk order, 0 = rows, 1 = breadth-first pages
   kTuneReduceRolling,       // order-exact reductions: 1 = rolling load pipeline, 0 = grouped
   kTuneOgsKernelGather,     // ogs gather: kernel variant as kTuneOgsKernel
   kTuneOgsKernelScatter,    // ogs scatter: kernel variant as kTuneOgsKernel
+  kTuneOgsRows,             // ogs plan: rows inside a warp chunk, 0 = CSR order, 1 = grouped by size
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -231,16 +231,63 @@ k_ogs_scatter(const int32_t* __restrict__ blocks, const int32_t* __restrict__ rs
 //
 // One warp per chunk of at most 256 non-zeros (a contiguous row range, see
 // sp_ogs_order.cpp).  Each lane loads 8 column ids and issues its 8 gathers before
-// using any of them; the values and the chunk's row starts go to the warp's own
+// using any of them; the values and the chunk's row bounds go to the warp's own
 // slice of shared memory; one lane per row combines in CSR order; results go back
 // coalesced.  Only __syncwarp separates the phases, so warps advance
 // independently and the SM keeps many chunks' loads in flight.
+//
+// Rows inside a chunk are processed either in CSR order (`grouped` = 0: `rs` is the
+// CSR row-start array, `ids` the CSR column ids) or grouped by size (`grouped` = 1:
+// `rs` holds build_grouped's packed words and `ids` the regrouped column ids).  In
+// both cases a row's members are combined in their CSR order, so the results are
+// the same bits; grouping only makes the 32 rows a warp runs side by side equally
+// long.  Descriptors are (r0, r1, g0, g1): rows [r0, r1), entries [g0, g1).
 
 template <typename T>
 struct WarpSmem {
   T val[kWarpsPerCta][kWarpChunkNnz];
   int32_t rs[kWarpsPerCta][kWarpChunkNnz + 8];
+  uint8_t ro[kWarpsPerCta][kWarpChunkNnz];
 };
+
+// Row r of chunk d (r < nr = d.y - d.x): its members are entries [a, b) of the
+// chunk and its row index is d.x + row.
+struct RowRef {
+  int32_t a, b, row;
+};
+
+// srs[r] (r <= nr): first entry of the r-th processed row relative to g0;
+// sro[r]: that row's offset from r0 (grouped order only).
+__device__ __forceinline__ void stage_rows(const int32_t* __restrict__ rs, int grouped, int4 d,
+                                           int lane, int32_t* srs, uint8_t* sro) {
+  const int32_t nr = d.y - d.x;
+  if (grouped) {
+    for (int32_t r = lane; r < nr; r += 32) {
+      const int32_t w = __ldg(rs + d.x + r);
+      srs[r] = w & 0xFFFF;
+      sro[r] = (uint8_t)(w >> 16);
+    }
+    if (lane == 0) srs[nr] = d.w - d.z;
+  } else {
+    for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + d.x + r) - d.z;
+  }
+}
+
+__device__ __forceinline__ RowRef staged_row(const int32_t* srs, const uint8_t* sro, int grouped,
+                                             int32_t r) {
+  return RowRef{srs[r], srs[r + 1], grouped ? (int32_t)sro[r] : r};
+}
+
+// Row r read straight from global memory (scatter kernels, which stage no values).
+__device__ __forceinline__ RowRef global_row(const int32_t* __restrict__ rs, int grouped, int4 d,
+                                             int32_t r) {
+  if (grouped) {
+    const int32_t w = __ldg(rs + d.x + r);
+    const int32_t b = (r + 1 < d.y - d.x) ? (__ldg(rs + d.x + r + 1) & 0xFFFF) : d.w - d.z;
+    return RowRef{w & 0xFFFF, b, w >> 16};
+  }
+  return RowRef{__ldg(rs + d.x + r) - d.z, __ldg(rs + d.x + r + 1) - d.z, r};
+}
 
 template <typename T>
 __device__ __forceinline__ void warp_stage(const int32_t* __restrict__ ids, int32_t g0, int32_t gn,
@@ -263,19 +310,18 @@ __device__ __forceinline__ void warp_stage(const int32_t* __restrict__ ids, int3
 template <typename T, int OP>
 __global__ void __launch_bounds__(kOgsThreads, 6)
 k_ogsw_gs_sym(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-              const int32_t* __restrict__ ids, T* __restrict__ v) {
+              const int32_t* __restrict__ ids, T* __restrict__ v, int grouped) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
   const int4 ch = __ldg(chunks + c);
-  const int32_t nr = ch.y - ch.x;
-  const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
+  const int32_t nr = ch.y - ch.x, gn = ch.w - ch.z;
   T* sv = sm.val[w];
   int32_t* srs = sm.rs[w];
-  for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + ch.x + r) - g0;
+  stage_rows(rs, grouped, ch, lane, srs, sm.ro[w]);
   int32_t col[kOgsPerLane];
-  warp_stage<T>(ids, g0, gn, v, sv, lane, col);
+  warp_stage<T>(ids, ch.z, gn, v, sv, lane, col);
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
     const int32_t a = srs[r], b = srs[r + 1];
@@ -291,49 +337,47 @@ k_ogsw_gs_sym(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 template <typename T, int OP>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-              const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv) {
+              const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv,
+              int grouped) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
   const int4 ch = __ldg(chunks + c);
-  const int32_t nr = ch.y - ch.x;
-  const int32_t g0 = __ldg(rs + ch.x), gn = __ldg(rs + ch.y) - g0;
+  const int32_t nr = ch.y - ch.x, gn = ch.w - ch.z;
   T* sv = sm.val[w];
-  int32_t* srs = sm.rs[w];
-  for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + ch.x + r) - g0;
+  stage_rows(rs, grouped, ch, lane, sm.rs[w], sm.ro[w]);
   int32_t col[kOgsPerLane];
-  warp_stage<T>(ids, g0, gn, v, sv, lane, col);
+  warp_stage<T>(ids, ch.z, gn, v, sv, lane, col);
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
-    const int32_t a = srs[r], b = srs[r + 1];
-    T acc = row_combine<T, OP>(sv, a, b);
-    gv[ch.x + r] = acc;
+    const RowRef q = staged_row(sm.rs[w], sm.ro[w], grouped, r);
+    gv[ch.x + q.row] = row_combine<T, OP>(sv, q.a, q.b);
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v) {
+               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
+               int grouped) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
   if (c >= nchunks) return;
   const int4 ch = __ldg(chunks + c);
-  const int32_t nr = ch.y - ch.x;
-  const int32_t s0 = __ldg(rs + ch.x), sn = __ldg(rs + ch.y) - s0;
+  const int32_t nr = ch.y - ch.x, sn = ch.w - ch.z;
   T* sv = sm.val[w];
   int32_t col[kOgsPerLane];
 #pragma unroll
   for (int u = 0; u < kOgsPerLane; ++u) {
     const int i = lane + 32 * u;
-    col[u] = (i < sn) ? __ldg(ids + s0 + i) : 0;
+    col[u] = (i < sn) ? __ldg(ids + ch.z + i) : 0;
   }
   for (int32_t r = lane; r < nr; r += 32) {
-    const T x = gv[ch.x + r];
-    const int32_t a = __ldg(rs + ch.x + r) - s0, b = __ldg(rs + ch.x + r + 1) - s0;
-    for (int32_t i = a; i < b; ++i) sv[i] = x;
+    const RowRef q = global_row(rs, grouped, ch, r);
+    const T x = gv[ch.x + q.row];
+    for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
   }
   __syncwarp();
 #pragma unroll
@@ -356,9 +400,9 @@ __device__ __forceinline__ void load_cols(const int32_t* __restrict__ ids, int4 
 }
 
 template <typename T, int OP, int MODE>  // MODE 0: gather+scatter (Sym), 1: gather
-__global__ void __launch_bounds__(kOgsThreads, 4)
+__global__ void __launch_bounds__(kOgsThreads, kOgsPersistentCtas)
 k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv) {
+              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
@@ -366,6 +410,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   if (c >= nchunks) return;
   T* sv = sm.val[w];
   int32_t* srs = sm.rs[w];
+  uint8_t* sro = sm.ro[w];
   const int4 zero = make_int4(0, 0, 0, 0);
   int4 d = __ldg(chunks + c);
   int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
@@ -378,7 +423,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 #pragma unroll
     for (int u = 0; u < kOgsPerLane; ++u)
       if (lane + 32 * u < gn) val[u] = v[col[u]];
-    for (int32_t r = lane; r <= nr; r += 32) srs[r] = __ldg(rs + d.x + r) - d.z;
+    stage_rows(rs, grouped, d, lane, srs, sro);
     int32_t coln[kOgsPerLane];
     load_cols(ids, dn, lane, coln);
 #pragma unroll
@@ -386,12 +431,12 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
       if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
     __syncwarp();
     for (int32_t r = lane; r < nr; r += 32) {
-      const int32_t a = srs[r], b = srs[r + 1];
-      T acc = row_combine<T, OP>(sv, a, b);
+      const RowRef q = staged_row(srs, sro, grouped, r);
+      T acc = row_combine<T, OP>(sv, q.a, q.b);
       if (MODE == 0) {
-        for (int32_t i = a; i < b; ++i) sv[i] = acc;
+        for (int32_t i = q.a; i < q.b; ++i) sv[i] = acc;
       } else {
-        gv[d.x + r] = acc;
+        gv[d.x + q.row] = acc;
       }
     }
     __syncwarp();
@@ -413,7 +458,8 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads, 4)
 k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v) {
+               const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
+               int grouped) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
@@ -431,9 +477,9 @@ k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     int32_t coln[kOgsPerLane];
     load_cols(ids, dn, lane, coln);
     for (int32_t r = lane; r < nr; r += 32) {
-      const T x = gv[d.x + r];
-      const int32_t a = __ldg(rs + d.x + r) - d.z, b = __ldg(rs + d.x + r + 1) - d.z;
-      for (int32_t i = a; i < b; ++i) sv[i] = x;
+      const RowRef q = global_row(rs, grouped, d, r);
+      const T x = gv[d.x + q.row];
+      for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
     }
     __syncwarp();
 #pragma unroll
@@ -449,9 +495,230 @@ k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
   }
 }
 
-static inline unsigned persistent_grid(int32_t nchunks) {
+// Asynchronously staged persistent variant (kernel 3): a chunk's gathered values
+// and row words are copied global -> shared with cp.async one chunk ahead, so
+// chunk c+W's gathers are in flight while chunk c is combined and written back.
+// Two buffers per warp; the column ids of chunk c+2W are loaded into registers a
+// further step ahead.  In gather+scatter mode chunk c+W's reads cannot see chunk
+// c's writes: every column belongs to exactly one row and every row to exactly
+// one chunk.
+__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void cp_async_val(T* smem, const T* gmem) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte values");
+  if constexpr (sizeof(T) == 8)
+    cp_async_8(smem, gmem);
+  else
+    cp_async_4(smem, gmem);
+}
+
+template <typename T>
+struct AsyncSmem {  // 48 KiB for 8-byte values
+  T val[kWarpsPerCta][2][kWarpChunkNnz];
+  int32_t rw[kWarpsPerCta][2][kWarpChunkNnz];  // row words as stored in `rs`
+};
+
+template <typename T>
+__device__ __forceinline__ void async_issue(const int32_t* __restrict__ rs, const T* v, int4 d,
+                                            const int32_t (&col)[kOgsPerLane], int lane, T* sv,
+                                            int32_t* srw) {
+  const int32_t gn = d.w - d.z, nr = d.y - d.x;
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < gn) cp_async_val<T>(sv + lane + 32 * u, v + col[u]);
+  for (int32_t r = lane; r < nr; r += 32) cp_async_4(srw + r, rs + d.x + r);
+}
+
+template <typename T, int OP, int MODE>  // MODE 0: gather+scatter (Sym), 1: gather
+__global__ void __launch_bounds__(kOgsThreads, 4)
+k_ogsa_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped) {
+  __shared__ AsyncSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  const int4 zero = make_int4(0, 0, 0, 0);
+  int4 d = __ldg(chunks + c);
+  int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  int32_t col[kOgsPerLane], coln[kOgsPerLane];
+  load_cols(ids, d, lane, col);
+  async_issue<T>(rs, v, d, col, lane, sm.val[w][0], sm.rw[w][0]);
+  cp_async_commit();
+  load_cols(ids, dn, lane, coln);
+  int buf = 0;
+  while (true) {
+    const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    // chunk c+W's copies (dn is all zeros past the end: nothing is issued)
+    async_issue<T>(rs, v, dn, coln, lane, sm.val[w][buf ^ 1], sm.rw[w][buf ^ 1]);
+    cp_async_commit();
+    int32_t colnn[kOgsPerLane];
+    load_cols(ids, dnn, lane, colnn);
+    cp_async_wait<1>();  // chunk c's group has landed
+    __syncwarp();
+    const T* sv = sm.val[w][buf];
+    const int32_t* srw = sm.rw[w][buf];
+    const int32_t gn = d.w - d.z, nr = d.y - d.x;
+    for (int32_t r = lane; r < nr; r += 32) {
+      const int32_t wa = srw[r];
+      const int32_t a = grouped ? (wa & 0xFFFF) : wa - d.z;
+      const int32_t b = (r + 1 < nr) ? (grouped ? (srw[r + 1] & 0xFFFF) : srw[r + 1] - d.z) : gn;
+      T acc = row_combine<T, OP>(sv, a, b);
+      if (MODE == 0) {
+        T* svw = sm.val[w][buf];
+        for (int32_t i = a; i < b; ++i) svw[i] = acc;
+      } else {
+        gv[d.x + (grouped ? (wa >> 16) : r)] = acc;
+      }
+    }
+    __syncwarp();
+    if (MODE == 0) {
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u)
+        if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
+      __syncwarp();  // buffer `buf` is refilled by the next iteration's copies
+    }
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+    dn = dnn;
+    buf ^= 1;
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u) {
+      col[u] = coln[u];
+      coln[u] = colnn[u];
+    }
+  }
+  cp_async_wait<0>();
+}
+
+// Column-order gathers (kernel 4 for gathers on T chunks), pipelined and persistent
+// like k_ogsp_gather: lane j of each pass loads the j-th smallest column of the
+// chunk, so a warp's loads (and, in gather+scatter mode, its stores) cover
+// neighbouring addresses; e2s maps each entry of the row walk to its slot, so every
+// row is still combined in CSR order from the op's identity (identical bits).
+template <typename T>
+struct SortedSmem {
+  T val[kWarpsPerCta][kWarpChunkNnz];
+  int32_t rs[kWarpsPerCta][kWarpChunkNnz + 8];
+  uint8_t ro[kWarpsPerCta][kWarpChunkNnz];
+  uint8_t e2s[kWarpsPerCta][kWarpChunkNnz];
+};
+
+template <typename T, int OP, int MODE>  // MODE 0: gather+scatter (Sym), 1: gather
+__global__ void __launch_bounds__(kOgsThreads, 4)
+k_ogso_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ colS, const uint8_t* __restrict__ e2s, T* v,
+              T* __restrict__ gv, int grouped) {
+  __shared__ SortedSmem<T> sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  T* sv = sm.val[w];
+  int32_t* srs = sm.rs[w];
+  uint8_t* sro = sm.ro[w];
+  uint8_t* se = sm.e2s[w];
+  const int4 zero = make_int4(0, 0, 0, 0);
+  int4 d = __ldg(chunks + c);
+  int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  int32_t col[kOgsPerLane];
+  load_cols(colS, d, lane, col);
+  while (true) {
+    const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    const int32_t gn = d.w - d.z, nr = d.y - d.x;
+    T val[kOgsPerLane];
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) val[u] = v[col[u]];
+    stage_rows(rs, grouped, d, lane, srs, sro);
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) se[lane + 32 * u] = __ldg(e2s + d.z + lane + 32 * u);
+    int32_t coln[kOgsPerLane];
+    load_cols(colS, dn, lane, coln);
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+    __syncwarp();
+    for (int32_t r = lane; r < nr; r += 32) {
+      const RowRef q = staged_row(srs, sro, grouped, r);
+      T acc = Op<T, OP>::init();
+      if (q.a < q.b) {
+        acc = Op<T, OP>::first(sv[se[q.a]]);
+        for (int32_t i = q.a + 1; i < q.b; ++i) Op<T, OP>::apply(acc, sv[se[i]]);
+      }
+      if (MODE == 0) {
+        for (int32_t i = q.a; i < q.b; ++i) sv[se[i]] = acc;
+      } else {
+        gv[d.x + q.row] = acc;
+      }
+    }
+    __syncwarp();
+    if (MODE == 0) {
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u)
+        if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
+      __syncwarp();
+    }
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+    dn = dnn;
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u) col[u] = coln[u];
+  }
+}
+
+// Column-order scatter (kernel 3 for scatters on T chunks): the chunk's row values
+// are read as one contiguous slice of gv into shared memory, then lane j of each
+// pass writes the j-th smallest column of the chunk.  Every load depends only on
+// the descriptor (one dependent round trip), there is no per-row loop, and the
+// stores of neighbouring lanes land on neighbouring addresses.  Copies only:
+// bit-identical to every other scatter.
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads, kOgsScatterCtas)
+k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ colS,
+               const uint8_t* __restrict__ rowOf, const T* __restrict__ gv, T* __restrict__ v) {
+  __shared__ T sres[kWarpsPerCta][kWarpChunkNnz];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;
+  const int4 d = __ldg(chunks + c);
+  const int32_t nr = d.y - d.x, sn = d.w - d.z;
+  T* sr = sres[w];
+  int32_t col[kOgsPerLane];
+  int32_t ro[kOgsPerLane];
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u) {
+    const int i = lane + 32 * u;
+    col[u] = (i < sn) ? __ldg(colS + d.z + i) : 0;
+    ro[u] = (i < sn) ? (int32_t)__ldg(rowOf + d.z + i) : 0;
+  }
+  for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[d.x + r];
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < kOgsPerLane; ++u)
+    if (lane + 32 * u < sn) v[col[u]] = sr[ro[u]];
+}
+
+static inline unsigned persistent_grid(int32_t nchunks, int ctas_per_sm = 4) {
   const int64_t want = ((int64_t)nchunks + kWarpsPerCta - 1) / kWarpsPerCta;
-  const int64_t cap = (int64_t)sm_count() * 4;
+  const int64_t cap = (int64_t)sm_count() * ctas_per_sm;
   return (unsigned)(want < cap ? (want < 1 ? 1 : want) : cap);
 }
 
@@ -460,25 +727,67 @@ static inline unsigned warp_grid(int32_t nchunks) {
 }
 
 // Kernel variant of an operation (knobs ogs.kernel / ogs.kernel.gather /
-// ogs.kernel.scatter): 0 block kernels, 1 warp chunks, 2 pipelined warp chunks.
-// The warp variants need k == 1 and a plan with chunks.
+// ogs.kernel.scatter): 0 block kernels, 1 warp chunks, 2 pipelined warp chunks,
+// 3 asynchronously staged warp chunks for the gathers and column-order warp chunks
+// for the scatter, 4 column-order pipelined gathers.  Launches through the N
+// operator take the pipelined kernels for the column-order variants.  The warp
+// variants need k == 1 and a plan with chunks.
 static inline int variant(TuneKey key, int K, int32_t nchunks) {
   return (K == 1 && nchunks > 0) ? (int)tune(key) : 0;
 }
 
+// The arrays one warp-chunk launch walks: T chunks use the grouped rows when the
+// plan has them; N chunks always use CSR order.
+struct ChunkArgs {
+  const int4* chunks;
+  int32_t nchunks;
+  const int32_t* rs;
+  const int32_t* ids;
+  int grouped;
+  const int32_t* colS;  // column-order entries (T chunks only, else null)
+  const uint8_t* e2s;
+};
+static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
+  const bool g = p->row_order == 1;
+  return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
+                   g ? p->d_rowsGT : p->d_rowStartsT, g ? p->d_colIdsGT : p->d_colIdsT, g ? 1 : 0,
+                   p->d_colIdsST, p->d_e2sT};
+}
+static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
+  return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
+                   p->d_colIdsN, 0, nullptr, nullptr};
+}
+
 // ------------------------------------------------------------------ dispatch
+
+template <typename T, int OP, int MODE>
+static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaStream_t s) {
+  if (kv == 4 && a.e2s) {
+    k_ogso_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+        a.chunks, a.nchunks, a.rs, a.colS, a.e2s, v, gv, a.grouped);
+  } else if (kv == 3) {
+    k_ogsa_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+        a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
+  } else if (kv >= 2) {
+    k_ogsp_gather<T, OP, MODE><<<persistent_grid(a.nchunks, kOgsPersistentCtas), kOgsThreads,
+                                 0, s>>>(
+        a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
+  } else if (MODE == 0) {
+    k_ogsw_gs_sym<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
+                                                                     a.ids, v, a.grouped);
+  } else {
+    k_ogsw_gather<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
+                                                                     a.ids, v, gv, a.grouped);
+  }
+}
 
 template <typename T, int OP>
 static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
-  if ((trans == SP_SYM || p->n_is_t) && variant(kTuneOgsKernel, K, p->nchunksT) == 2) {
-    k_ogsp_gather<T, OP, 0><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
-        v, nullptr);
-  } else if ((trans == SP_SYM || p->n_is_t) && variant(kTuneOgsKernel, K, p->nchunksT) == 1) {
-    k_ogsw_gs_sym<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT, v);
+  const int kv = variant(kTuneOgsKernel, K, p->nchunksT);
+  if ((trans == SP_SYM || p->n_is_t) && kv > 0) {
+    launch_chunked_gather<T, OP, 0>(kv, chunks_t(p), v, nullptr, s);
   } else if (trans == SP_SYM || p->n_is_t) {
     k_ogs_gs_sym<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
                                                      v, K);
@@ -495,23 +804,12 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
 template <typename T, int OP>
 static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
                           cudaStream_t s) {
-  if (trans == SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksN) == 2) {
-    k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-        p->d_colIdsN, const_cast<T*>(v), gv);
-  } else if (trans != SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksT) == 2) {
-    k_ogsp_gather<T, OP, 1><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
-        const_cast<T*>(v), gv);
-  } else if (trans == SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksN) == 1) {
-    k_ogsw_gather<T, OP><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-        p->d_colIdsN, v, gv);
-  } else if (trans != SP_NOTRANS && variant(kTuneOgsKernelGather, K, p->nchunksT) == 1) {
-    k_ogsw_gather<T, OP><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
-        v, gv);
-  } else if (trans == SP_NOTRANS) {
+  const bool useN = (trans == SP_NOTRANS);
+  const int kv = variant(kTuneOgsKernelGather, K, useN ? p->nchunksN : p->nchunksT);
+  if (kv > 0) {
+    launch_chunked_gather<T, OP, 1>(kv, useN ? chunks_n(p) : chunks_t(p), const_cast<T*>(v), gv,
+                                    s);
+  } else if (useN) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_gather<T, OP><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
         p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, v, gv, K);
@@ -525,23 +823,21 @@ static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv
 template <typename T>
 static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, const T* gv,
                            cudaStream_t s) {
-  if (trans == SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksN) == 2) {
-    k_ogsp_scatter<T><<<persistent_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-        p->d_colIdsN, gv, v);
-  } else if (trans != SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksT) == 2) {
-    k_ogsp_scatter<T><<<persistent_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
-        gv, v);
-  } else if (trans == SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksN) == 1) {
-    k_ogsw_scatter<T><<<warp_grid(p->nchunksN), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-        p->d_colIdsN, gv, v);
-  } else if (trans != SP_TRANS && variant(kTuneOgsKernelScatter, K, p->nchunksT) == 1) {
-    k_ogsw_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_rowStartsT, p->d_colIdsT,
-        gv, v);
-  } else if (trans == SP_TRANS) {
+  const bool useN = (trans == SP_TRANS);
+  const int kv = variant(kTuneOgsKernelScatter, K, useN ? p->nchunksN : p->nchunksT);
+  if (kv == 3 && !useN && p->d_colIdsST) {
+    k_ogss_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv,
+        v);
+  } else if (kv > 0) {
+    const ChunkArgs a = useN ? chunks_n(p) : chunks_t(p);
+    if (kv >= 2)
+      k_ogsp_scatter<T><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped);
+    else
+      k_ogsw_scatter<T><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
+                                                                     a.ids, gv, v, a.grouped);
+  } else if (useN) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_scatter<T><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
         p->d_blocksN, p->d_rowStartsNpad, p->d_colIdsN, gv, v, K);
@@ -637,6 +933,15 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->d_chunksT = p->d_chunksN = nullptr;
   p->nchunksT = p->nchunksN = 0;
   p->own_chunks_n = false;
+  if (p->d_rowsGT) cudaFree(p->d_rowsGT);
+  if (p->d_colIdsGT) cudaFree(p->d_colIdsGT);
+  p->d_rowsGT = p->d_colIdsGT = nullptr;
+  p->row_order = 0;
+  if (p->d_colIdsST) cudaFree(p->d_colIdsST);
+  if (p->d_rowOfST) cudaFree(p->d_rowOfST);
+  if (p->d_e2sT) cudaFree(p->d_e2sT);
+  p->d_colIdsST = nullptr;
+  p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
   for (int32_t* q : ptrs)
     if (q) cudaFree(q);
@@ -645,15 +950,16 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->own_n_csr = p->own_blocks_n = false;
 }
 
-static sp_status upload(const std::vector<int32_t>& h, int32_t** d, cudaStream_t s) {
-  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(int32_t);
+template <typename E>
+static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
+  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(E);
   if (cudaMalloc(d, bytes) != cudaSuccess) {
     cudaGetLastError();
     *d = nullptr;
     return fail(SP_ERR_ALLOC, "ogs plan: cudaMalloc of %zu bytes failed", bytes);
   }
-  if (!h.empty()) SP_CUDA_TRY(cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(int32_t),
-                                              cudaMemcpyHostToDevice, s));
+  if (!h.empty())
+    SP_CUDA_TRY(cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(E), cudaMemcpyHostToDevice, s));
   return SP_SUCCESS;
 }
 
@@ -756,6 +1062,23 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       p->own_chunks_n = true;
       if ((st = upload(chunksN, &p->d_chunksN, s))) return st;
     }
+    // T rows grouped by size inside each chunk (the N operator keeps CSR order)
+    std::vector<int32_t> rowsG, colIdsG;
+    if (tune(kTuneOgsRows) == 1 && p->nchunksT > 0) {
+      build_grouped(chunksT, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), rowsG, colIdsG);
+      if ((st = upload(rowsG, &p->d_rowsGT, s))) return st;
+      if ((st = upload(colIdsG, &p->d_colIdsGT, s))) return st;
+      p->row_order = 1;
+    }
+    // T chunk entries in column order: the column-order scatter and gathers
+    std::vector<int32_t> colS;
+    std::vector<uint8_t> rowOf, e2s;
+    build_sorted(chunksT, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(),
+                 p->row_order == 1 ? colIdsG.data() : p->colIdsT.data(), colS, rowOf, e2s);
+    if ((st = upload(colS, &p->d_colIdsST, s))) return st;
+    if ((st = upload(rowOf, &p->d_rowOfST, s))) return st;
+    if ((st = upload(e2s, &p->d_e2sT, s))) return st;
+    SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   }
   SP_CUDA_TRY(cudaStreamSynchronize(s));
   return SP_SUCCESS;
@@ -839,6 +1162,7 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->NchunksT = p->nchunksT;
   info->NchunksN = p->nchunksN;
   info->chunkOrder = p->chunk_order;
+  info->rowOrder = p->row_order;
   return SP_SUCCESS;
 }
 

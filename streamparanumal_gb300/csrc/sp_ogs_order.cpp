@@ -123,4 +123,54 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
   return true;
 }
 
+void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rs,
+                   const int32_t* ci, std::vector<int32_t>& rowsG, std::vector<int32_t>& ciG) {
+  const int64_t nchunks = (int64_t)quads.size() / 4;
+  rowsG.assign(nrows, 0);
+  ciG.assign(nrows > 0 ? rs[nrows] : 0, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int32_t r0 = quads[4 * c], r1 = quads[4 * c + 1], g0 = quads[4 * c + 2];
+    int32_t order[kWarpChunkNnz];
+    const int32_t nr = r1 - r0;
+    for (int32_t k = 0; k < nr; ++k) order[k] = k;
+    std::stable_sort(order, order + nr, [&](int32_t a, int32_t b) {
+      return rs[r0 + a + 1] - rs[r0 + a] > rs[r0 + b + 1] - rs[r0 + b];
+    });
+    int32_t at = g0;
+    for (int32_t k = 0; k < nr; ++k) {
+      const int32_t r = r0 + order[k];
+      rowsG[r0 + k] = (at - g0) | (order[k] << 16);
+      for (int32_t i = rs[r]; i < rs[r + 1]; ++i) ciG[at++] = ci[i];
+    }
+  }
+}
+
+void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rs,
+                  const int32_t* ci, const int32_t* ciE, std::vector<int32_t>& colS,
+                  std::vector<uint8_t>& rowOf, std::vector<uint8_t>& e2s) {
+  const int64_t nchunks = (int64_t)quads.size() / 4;
+  const int32_t nnz = nrows > 0 ? rs[nrows] : 0;
+  colS.assign(nnz, 0);
+  rowOf.assign(nnz, 0);
+  e2s.assign(nnz, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int32_t r0 = quads[4 * c], r1 = quads[4 * c + 1], g0 = quads[4 * c + 2];
+    int64_t key[kWarpChunkNnz];  // column << 8 | row offset: sorts by column
+    int32_t n = 0;
+    for (int32_t r = r0; r < r1; ++r)
+      for (int32_t i = rs[r]; i < rs[r + 1]; ++i) key[n++] = ((int64_t)ci[i] << 8) | (r - r0);
+    std::sort(key, key + n);
+    int32_t* cs = colS.data() + g0;
+    for (int32_t j = 0; j < n; ++j) {
+      cs[j] = (int32_t)(key[j] >> 8);
+      rowOf[g0 + j] = (uint8_t)(key[j] & 0xFF);
+    }
+    // every column appears once in a chunk, so its sorted position is unique
+    for (int32_t e = 0; e < n; ++e)
+      e2s[g0 + e] = (uint8_t)(std::lower_bound(cs, cs + n, ciE[g0 + e]) - cs);
+  }
+}
+
 }  // namespace sp

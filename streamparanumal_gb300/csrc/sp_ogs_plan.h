@@ -17,6 +17,17 @@ constexpr int kOgsMaxRowSize = 512;
 // Warp chunks: at most 256 non-zeros (8 per lane) and 256 rows, one warp each.
 constexpr int kWarpChunkNnz = 256;
 constexpr int kWarpsPerCta = 8;
+// Resident CTAs per SM that the pipelined persistent gathers are compiled for (a
+// register budget of 65536 / (256 * n) per lane) and launched with, and the
+// register cap of the column-order scatter (1 = none).  Build-time tuning values.
+#ifndef SP_OGS_PERSISTENT_CTAS
+#define SP_OGS_PERSISTENT_CTAS 4
+#endif
+#ifndef SP_OGS_SCATTER_CTAS
+#define SP_OGS_SCATTER_CTAS 1
+#endif
+constexpr int kOgsPersistentCtas = SP_OGS_PERSISTENT_CTAS;
+constexpr int kOgsScatterCtas = SP_OGS_SCATTER_CTAS;
 
 struct OgsOperatorDev {
   int32_t nrows = 0;       // rows covered by `blocks`
@@ -35,6 +46,30 @@ bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t
 // local data.  Returns false when a row holds more than kWarpChunkNnz entries.
 bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
                   int order, std::vector<int32_t>& chunks);
+
+// Rows of every chunk regrouped by size.  `quads` holds the chunk descriptors
+// (r0, r1, g0, g1).  Inside chunk [r0, r1) the rows are reordered by member count,
+// largest first (ties in row order), and their members are laid out in that order
+// over the chunk's own entry range [g0, g1), each row's members keeping their CSR
+// order.  rowsG[r0 + k] = (offset of the k-th grouped row's first member from g0)
+// | (its row - r0) << 16; colIdsG holds the regrouped column ids.  One warp then
+// runs rows of equal size side by side, so its lanes finish their row loops
+// together.
+void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rowStarts,
+                   const int32_t* colIds, std::vector<int32_t>& rowsG,
+                   std::vector<int32_t>& colIdsG);
+
+// Entries of every chunk in ascending column order, for kernels that touch local
+// data in address order.  For chunk (r0, r1, g0, g1): colIdsS[g0 + j] is the j-th
+// smallest column of the chunk and rowOfS[g0 + j] the offset from r0 of the row it
+// belongs to (a scatter writes v[colIdsS[j]] = gv[r0 + rowOfS[j]] with neighbouring
+// lanes on neighbouring addresses, and needs no row bounds).  `colIdsE` lists the
+// chunk's entries in the order the row bounds walk them (CSR order, or grouped by
+// size); e2s[g0 + e] is the sorted position of entry e of that order, so a gather
+// can load values in column order and still combine each row in CSR order.
+void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rowStarts,
+                  const int32_t* colIds, const int32_t* colIdsE, std::vector<int32_t>& colIdsS,
+                  std::vector<uint8_t>& rowOfS, std::vector<uint8_t>& e2s);
 
 }  // namespace sp
 
@@ -63,6 +98,15 @@ struct sp_ogs_plan {
   int32_t nchunksT = 0, nchunksN = 0;
   bool own_chunks_n = false;
   int32_t chunk_order = 0;
+  // T rows regrouped by size inside each T chunk (build_grouped); null when the
+  // plan keeps CSR order (knob ogs.rows = 0) or has no chunks
+  int32_t* d_rowsGT = nullptr;       // NrowsT packed (start offset | row offset << 16)
+  int32_t* d_colIdsGT = nullptr;     // nnzT
+  int32_t row_order = 0;             // 1 when d_rowsGT / d_colIdsGT are in use
+  // T chunk entries in column order (build_sorted), for the column-order scatter
+  int32_t* d_colIdsST = nullptr;     // nnzT
+  uint8_t* d_rowOfST = nullptr;      // nnzT
+  uint8_t* d_e2sT = nullptr;         // nnzT: sorted position of each row-order entry
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
   bool own_blocks_n = false;      // d_blocksN is a separate allocation
 

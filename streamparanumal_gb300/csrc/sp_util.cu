@@ -33,11 +33,12 @@ struct TuneEntry {
 static TuneEntry g_tune[kTuneCount] = {
     {"reduce.prefetch_chunks", -1, 64, {-1}},
     {"ogs.block_nnz", 256, 2048, {2048}},
-    {"ogs.kernel", 0, 2, {2}},
+    {"ogs.kernel", 0, 4, {2}},
     {"ogs.order", 0, 1, {1}},
     {"reduce.rolling", 0, 1, {1}},
-    {"ogs.kernel.gather", 0, 2, {2}},
-    {"ogs.kernel.scatter", 0, 2, {1}},
+    {"ogs.kernel.gather", 0, 4, {2}},
+    {"ogs.kernel.scatter", 0, 3, {3}},
+    {"ogs.rows", 0, 1, {1}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -182,21 +182,34 @@ def test_large_block_boundaries(cuda, orc):
     assert h.info.maxRowSize == sizes.max()
 
 
-@pytest.mark.parametrize("kernel,order", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
+VARIANTS = [(0, 0, 0), (1, 0, 0), (1, 1, 1), (2, 0, 0), (2, 1, 0), (2, 1, 1), (3, 0, 1),
+            (3, 1, 0), (3, 1, 1), (4, 0, 0), (4, 1, 0), (4, 1, 1)]
+KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.kernel.scatter", "ogs.order", "ogs.rows")
+
+
+def set_variant(kernel, order, rows):
+    capi.tune_set("ogs.kernel", kernel)
+    capi.tune_set("ogs.kernel.gather", kernel)
+    capi.tune_set("ogs.kernel.scatter", min(kernel, 3))
+    capi.tune_set("ogs.order", order)
+    capi.tune_set("ogs.rows", rows)
+
+
+@pytest.mark.parametrize("kernel,order,rows", VARIANTS)
 @pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0)])
-def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
-    """Block kernels, and warp-chunk kernels in row and breadth-first order, all give
-    the reference's bits (each row is still summed by one lane in CSR order)."""
+def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, rows, box):
+    """Block kernels, warp-chunk kernels (plain, pipelined, asynchronously staged
+    gathers, column-order scatter and gathers) in row and breadth-first chunk order,
+    with rows in CSR order or grouped by size: all give the reference's bits (each
+    row is still summed by one lane in CSR order)."""
     nx, ny, nz, p, seed = box
-    keys = ("ogs.kernel", "ogs.kernel.gather", "ogs.kernel.scatter", "ogs.order")
-    old = {k: capi.tune_get(k) for k in keys}
+    old = {k: capi.tune_get(k) for k in KNOBS}
     try:
-        for k in keys[:3]:
-            capi.tune_set(k, kernel)
-        capi.tune_set("ogs.order", order)
+        set_variant(kernel, order, rows)
         ids = O.box_hex_ids(nx, ny, nz, p, seed)
         h, ref = make(orc, ids)
         assert h.info.chunkOrder == order and h.info.NchunksT > 0
+        assert h.info.rowOrder == rows
         rs, ci = ref["rsT"], ref["ciT"]
         q = orc.uniform(ids.size, 91)
         gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
@@ -212,6 +225,39 @@ def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, box):
         gN = torch.zeros(ref["rsN"].size - 1, dtype=torch.float64, device="cuda")
         h.Gather(gN, torch.from_numpy(q).cuda(), 1, O.Add, O.NoTrans)
         np.testing.assert_array_equal(host(gN), orc.gather(ref["rsN"], ref["ciN"], q))
+    finally:
+        for k, v in old.items():
+            capi.tune_set(k, v)
+
+
+@pytest.mark.parametrize("kernel,rows", [(2, 1), (3, 0), (3, 1), (4, 0), (4, 1)])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
+@pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
+def test_variants_types_ops(cuda, orc, kernel, rows, dtype, op):
+    """Every type and op through the warp-chunk variants with grouped rows, the
+    asynchronously staged gathers (4- and 8-byte cp.async copies) and the
+    column-order scatter and gathers."""
+    old = {k: capi.tune_get(k) for k in KNOBS}
+    try:
+        set_variant(kernel, 1, rows)
+        ids = O.box_hex_ids(4, 3, 5, 3, 77)
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        rng = np.random.default_rng(5)
+        if dtype == torch.float32:
+            q = rng.uniform(-1, 1, ids.size).astype(np.float32)
+        else:
+            q = rng.integers(-9, 10, ids.size).astype(np.int32 if dtype == torch.int32 else np.int64)
+        gq = torch.zeros(rs.size - 1, dtype=dtype, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, op, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q, 1, op))
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, op, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op))
+        g = orc.gather(rs, ci, q, 1, op)
+        dq = torch.zeros(ids.size, dtype=dtype, device="cuda")
+        h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)
+        np.testing.assert_array_equal(host(dq), orc.scatter(rs, ci, g, np.zeros_like(q)))
     finally:
         for k, v in old.items():
             capi.tune_set(k, v)
