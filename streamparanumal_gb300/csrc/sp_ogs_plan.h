@@ -18,13 +18,14 @@ constexpr int kOgsMaxRowSize = 512;
 constexpr int kWarpChunkNnz = 256;
 constexpr int kWarpsPerCta = 8;
 // Resident CTAs per SM that the pipelined persistent gathers are compiled for (a
-// register budget of 65536 / (256 * n) per lane) and launched with, and the
-// register cap of the column-order scatter (1 = none).  Build-time tuning values.
+// register budget of 65536 / (256 * n) per lane) and launched with, and the one
+// the column-order scatter is compiled for.  Build-time tuning values; GB300
+// sweeps of the 64^3 p=7 box (3..6 and 5..8) put the optimum at 4 and 5.
 #ifndef SP_OGS_PERSISTENT_CTAS
 #define SP_OGS_PERSISTENT_CTAS 4
 #endif
 #ifndef SP_OGS_SCATTER_CTAS
-#define SP_OGS_SCATTER_CTAS 1
+#define SP_OGS_SCATTER_CTAS 5
 #endif
 constexpr int kOgsPersistentCtas = SP_OGS_PERSISTENT_CTAS;
 constexpr int kOgsScatterCtas = SP_OGS_SCATTER_CTAS;
