@@ -30,6 +30,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "BS1-8 HBM GB/s (reference byte accounting), FP64 suite"
 UNIT = "GB/s"
+E2E_REPEATS = 5
 
 
 def parse():
@@ -300,14 +301,16 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     t_setup = time.time()
     h_a = torch.from_numpy(orc.uniform(N, args.seed)).pin_memory()
     h_b = torch.from_numpy(orc.uniform(N, args.seed + 1)).pin_memory()
-    ids = O.box_hex_ids(mesh, mesh, mesh, p, args.perm_seed)
-    Nt = ids.size
-    h_q = torch.from_numpy(orc.uniform(Nt, args.seed + 2)).pin_memory()
+    # mesh ids and the gather-scatter plan, both built on the device
+    t_plan = time.time()
+    ids = O.box_hex_ids(mesh, mesh, mesh, p, args.perm_seed, device=dev, stream=stream)
+    Nt = ids.numel()
     h = O.ogs_t()
-    with torch.cuda.stream(stream):
-        h.Setup(Nt, ids, kind=O.Signed, unique=True, stream=stream)
+    h.Setup(Nt, ids, kind=O.Signed, unique=True, stream=stream)
     Ng = h.NgatherGlobal
     del ids
+    t_plan = time.time() - t_plan
+    h_q = torch.from_numpy(orc.uniform(Nt, args.seed + 2)).pin_memory()
     a = h_a.to(dev)
     b = h_b.to(dev)
     q = h_q.to(dev)
@@ -412,7 +415,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     h_out_b = torch.empty_like(h_b).pin_memory()
     h_out_q = torch.empty_like(h_q).pin_memory()
     h_scal = torch.empty(4, dtype=torch.float64).pin_memory()
-    e2e_steps = max(3, min(args.steps, 20))
+    e2e_steps = max(3, min(args.steps, 10))
     sets = [(a, b, q, scal), (torch.empty_like(a), torch.empty_like(b), torch.empty_like(q),
                               torch.zeros_like(scal))]
     s_in = torch.cuda.Stream(device=dev)
@@ -461,15 +464,20 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
     e2e_run(2)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    if dist:
-        tdist.barrier()
-    e0.record(stream)
-    e2e_run(e2e_steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, dev)
+    # the host link is shared with the machine's other work, so the pipeline is
+    # timed E2E_REPEATS times and the median run is reported (all runs are listed)
+    e2e_runs = []
+    for _ in range(E2E_REPEATS):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if dist:
+            tdist.barrier()
+        e0.record(stream)
+        e2e_run(e2e_steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_runs.append(max_over_ranks(e0.elapsed_time(e1) / e2e_steps, dev))
+    e2e_ms = statistics.median(e2e_runs)
     h2d = (h_a.numel() + h_b.numel() + h_q.numel()) * 8
     d2h = (h_out_b.numel() + h_out_q.numel() + h_scal.numel()) * 8
     e2e_value = job_rate(world, step_bytes, e2e_ms)
@@ -503,13 +511,15 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                      "peak_source": peak_kind, "traffic": traffic},
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3),
-                "steps": e2e_steps,
+                "steps": e2e_steps, "repeats": E2E_REPEATS,
+                "runs_ms_per_step": [round(x, 3) for x in e2e_runs],
                 "pipeline": "double-buffered: step k+1 uploads and step k-1 downloads "
                             "overlap step k's kernels (pinned host buffers, copy engines)"},
         "gpu_launches": launches,
         "clocks": clocks,
         "detail": {"per_kernel": detail, "bs0_us_per_launch": bs0,
-                   "storage_forms": forms, "setup_s": round(t_setup, 2)},
+                   "storage_forms": forms, "setup_s": round(t_setup, 2),
+                   "mesh_and_plan_s": round(t_plan, 2)},
     }
     if not args.no_cpu_baseline:
         gbs, desc, cores, _, _ = cpu_sample(args.cpu_nlog2, args.cpu_mesh, p, args.perm_seed,
@@ -792,14 +802,15 @@ def run_degree_sweep(args, local_rank: int) -> None:
     for p in _degrees(args.degree_sweep):
         E = int(round((args.sweep_nodes / (p + 1) ** 3) ** (1.0 / 3.0)))
         for perm in (0, args.perm_seed):
-            ids = O.box_hex_ids(E, E, E, p, perm)
+            ids = O.box_hex_ids(E, E, E, p, perm, device="cuda")
             res = autotune.tune_ogs(E, p, perm, ids=ids)
             autotune.record(table, res)
             best = res["best"]
             autotune.apply(p, bool(perm), table)
             h = O.ogs_t()
-            h.Setup(ids.size, ids, unique=True)
-            Nt, Ng = ids.size, h.NgatherGlobal
+            h.Setup(ids.numel(), ids, unique=True)
+            Nt, Ng = ids.numel(), h.NgatherGlobal
+            del ids
             line = {"metric": "BS6-BS8 GB/s per degree (reference byte accounting)", "p": p,
                     "E": E, "layout": "permuted" if perm else "lexicographic",
                     "local_nodes": Nt, "global_nodes": Ng, "tuned": best, "peak": peak,

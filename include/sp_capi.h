@@ -65,9 +65,10 @@ void        sp_launch_count_reset(void);
  *    order-exact reductions;
  *  "ogs.block_nnz" (256..2048, default 2048): non-zeros per row block of plans
  *    created afterwards;
- *  "ogs.order" (0 row order, 1 breadth-first over 4 KiB pages; default 1) and
- *    "ogs.rows" (0 CSR order, 1 rows grouped by size inside a chunk; default 1) for
- *    the warp chunks of plans created afterwards;
+ *  "ogs.order" (0 row order, 1 breadth-first over pages of local data; default 1),
+ *    "ogs.page_shift" (3..16, default 9: pages of 2^9 entries) and "ogs.rows" (0
+ *    CSR order, 1 rows grouped by size inside a chunk; default 1) for the warp
+ *    chunks of plans created afterwards;
  *  "ogs.kernel" / "ogs.kernel.gather" / "ogs.kernel.scatter" (gather+scatter /
  *    gather / scatter): 0 block kernels, 1 warp-chunk kernels, 2 pipelined
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
@@ -201,7 +202,7 @@ typedef struct {
   int64_t NgatherGlobal;
   int32_t NchunksT;   /* warp chunks of the T / N operators (0: block kernels only) */
   int32_t NchunksN;
-  int32_t chunkOrder; /* 0 row order, 1 breadth-first over 4 KiB pages             */
+  int32_t chunkOrder; /* 0 row order, 1 breadth-first over pages of local data      */
   int32_t rowOrder;   /* T rows inside a chunk: 0 CSR order, 1 grouped by size      */
 } sp_ogs_info;
 
@@ -211,6 +212,12 @@ typedef struct {
  * (as the reference does).  Host-side setup plus device upload on `stream`. */
 sp_status sp_ogs_setup(int32_t N, int64_t* h_ids, sp_kind kind, int32_t unique,
                        sp_stream_t stream, sp_ogs_plan** out);
+/* The same setup with the ids in device memory (d_ids[N], signs written back there
+ * with unique): grouping, owner draws, row numbering and CSR built on the GPU
+ * (same plan as sp_ogs_setup), for meshes whose ids are generated on the device.
+ * Allocates scratch of about 60 bytes per id; synchronises `stream`. */
+sp_status sp_ogs_setup_device(int32_t N, int64_t* d_ids, sp_kind kind, int32_t unique,
+                              sp_stream_t stream, sp_ogs_plan** out);
 /* Host half of sp_ogs_setup: fills the T and N CSR without touching the device.
  * rowStarts* need N+1 entries and colIds* N entries. */
 sp_status sp_ogs_setup_csr(int32_t N, int64_t* h_ids, sp_kind kind, int32_t unique,
@@ -275,6 +282,11 @@ sp_status sp_batch_destroy(sp_batch* b);
  * stream), slot(e) = perm[e].  h_ids must hold nx*ny*nz*(p+1)^3 entries. */
 sp_status sp_mesh_box_hex_ids(int32_t nx, int32_t ny, int32_t nz, int32_t p, uint64_t perm_seed,
                               int64_t* h_ids);
+/* The same ids written into device memory d_ids by a kernel (one thread per local
+ * node takes the minimum over the up to 8 element nodes on its lattice point);
+ * synchronises `stream`. */
+sp_status sp_mesh_box_hex_ids_device(int32_t nx, int32_t ny, int32_t nz, int32_t p,
+                                     uint64_t perm_seed, int64_t* d_ids, sp_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -22,11 +22,22 @@ from . import ogs as O
 
 TABLE = Path(__file__).resolve().parent / "tuning" / "gb300.json"
 
-# (plan-time knobs) x (launch-time kernel): plans are rebuilt only when order, rows
-# or block_nnz change
+# (plan-time knobs) x (launch-time kernel): plans are rebuilt only when order, rows,
+# page_shift or block_nnz change
 PLAN_CONFIGS = [{"order": 1, "rows": 1, "block_nnz": 2048}, {"order": 1, "rows": 0, "block_nnz": 2048},
                 {"order": 0, "rows": 1, "block_nnz": 2048}, {"order": 0, "rows": 0, "block_nnz": 2048},
                 {"order": 0, "rows": 0, "block_nnz": 1024}]
+DEFAULT_PAGE_SHIFT = 9
+
+
+def plan_configs(p: int) -> list[dict]:
+    """PLAN_CONFIGS with the default 512-entry pages, plus breadth-first pages of
+    about one element ((p+1)^3 entries) when that size differs."""
+    shift = max(3, ((p + 1) ** 3 - 1).bit_length())
+    cfgs = [dict(c, page_shift=DEFAULT_PAGE_SHIFT) for c in PLAN_CONFIGS]
+    if shift != DEFAULT_PAGE_SHIFT:
+        cfgs.insert(1, {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": shift})
+    return cfgs
 KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
            3: "warp-async-staged gathers / column-order scatter", 4: "column-order gathers"}
 OPS = (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs"))
@@ -45,7 +56,8 @@ def _time(fn, reps: int, stream) -> float:
     return e0.elapsed_time(e1) / reps
 
 
-KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "block_nnz": "ogs.block_nnz",
+KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift",
+         "block_nnz": "ogs.block_nnz",
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
          "kernel_scatter": "ogs.kernel.scatter"}
 
@@ -71,21 +83,21 @@ def _kernels(pc: dict, op: str) -> list[int]:
 
 def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
              ids=None) -> dict:
-    """Times every variant of BS6 / BS7 / BS8 on an E^3 box of degree p; the winner
-    takes, for the best (chunk order, row grouping), the fastest kernel of each
-    operation."""
+    """Times every variant of BS6 / BS7 / BS8 on an E^3 box of degree p (ids: numpy
+    or CUDA tensor; built on the device when omitted); the winner takes, for the
+    best (chunk order, row grouping), the fastest kernel of each operation."""
     saved = {k: capi.tune_get(knob) for k, knob in KNOBS.items()}
     stream = torch.cuda.current_stream()
     if ids is None:
-        ids = O.box_hex_ids(E, E, E, p, perm_seed)
-    Nt = ids.size
+        ids = O.box_hex_ids(E, E, E, p, perm_seed, device="cuda")
+    Nt = ids.numel() if isinstance(ids, torch.Tensor) else ids.size
     q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
-    timings = []  # (order, rows, block_nnz, kernel, op, ms)
+    timings = []  # (order, rows, page_shift, block_nnz, kernel, op, ms)
     try:
-        for pc in PLAN_CONFIGS:
+        for pc in plan_configs(p):
             _set(pc)
             h = O.ogs_t()
-            h.Setup(Nt, ids.copy(), unique=True)
+            h.Setup(Nt, ids.clone() if isinstance(ids, torch.Tensor) else ids.copy(), unique=True)
             gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
             ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
                    "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
@@ -93,19 +105,18 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
             for op, key in OPS:
                 for k in _kernels(pc, op):
                     _set({key: k})
-                    timings.append((pc["order"], pc["rows"], pc["block_nnz"], k, op,
-                                    _time(ops[op], reps, stream)))
+                    timings.append((pc["order"], pc["rows"], pc["page_shift"], pc["block_nnz"], k,
+                                    op, _time(ops[op], reps, stream)))
             h.Free()
             del gq
     finally:
         _set(saved)
     best_total, best = None, None
-    for order, rows in sorted({(t[0], t[1]) for t in timings}):
-        choice, total = {"order": order, "rows": rows}, 0.0
+    for order, rows, shift in sorted({t[:3] for t in timings}):
+        choice, total = {"order": order, "rows": rows, "page_shift": shift}, 0.0
         for op, key in OPS:
-            cands = [t for t in timings
-                     if t[4] == op and ((t[0], t[1]) == (order, rows) or t[3] == 0)]
-            _, _, bnnz, k, _, ms = min(cands, key=lambda t: t[5])
+            cands = [t for t in timings if t[5] == op and (t[:3] == (order, rows, shift) or t[4] == 0)]
+            _, _, _, bnnz, k, _, ms = min(cands, key=lambda t: t[6])
             choice[key] = k
             if k == 0:
                 choice["block_nnz"] = bnnz
@@ -115,8 +126,8 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
     best.setdefault("block_nnz", 2048)
     return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,
             "best_total_ms": best_total,
-            "candidates": [{"order": o, "rows": r, "block_nnz": b, "kernel": k, "op": op, "ms": ms}
-                           for o, r, b, k, op, ms in timings]}
+            "candidates": [{"order": o, "rows": r, "page_shift": ps, "block_nnz": b, "kernel": k,
+                            "op": op, "ms": ms} for o, r, ps, b, k, op, ms in timings]}
 
 
 def load_table(path: Path = TABLE) -> dict:

@@ -87,6 +87,7 @@ SIGNATURES = {
     "sp_ogs_setup_csr": (c_int32, [c_int32, _I64P, c_int32, c_int32, _I32P, _I32P, _I32P,
                                    _I32P, _I32P, _I32P]),
     "sp_ogs_setup": (c_int32, [c_int32, _I64P, c_int32, c_int32, _P, POINTER(c_void_p)]),
+    "sp_ogs_setup_device": (c_int32, [c_int32, _P, c_int32, c_int32, _P, POINTER(c_void_p)]),
     "sp_ogs_plan_create": (c_int32, [c_int32, c_int32, _I32P, _I32P, c_int32, _I32P, _I32P,
                                      _P, POINTER(c_void_p)]),
     "sp_ogs_plan_destroy": (c_int32, [_P]),
@@ -101,6 +102,8 @@ SIGNATURES = {
     "sp_batch_run": (c_int32, [_P, _P]),
     "sp_batch_destroy": (c_int32, [_P]),
     "sp_mesh_box_hex_ids": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _I64P]),
+    "sp_mesh_box_hex_ids_device": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _P,
+                                             _P]),
 }
 
 _STATUS_FREE = {"sp_last_error_string", "sp_status_string", "sp_version", "sp_launch_count",

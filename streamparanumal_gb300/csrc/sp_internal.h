@@ -48,6 +48,7 @@ enum TuneKey : int {
   kTuneOgsKernelGather,     // ogs gather: kernel variant as kTuneOgsKernel
   kTuneOgsKernelScatter,    // ogs scatter: kernel variant as kTuneOgsKernel
   kTuneOgsRows,             // ogs plan: rows inside a warp chunk, 0 = CSR order, 1 = grouped by size
+  kTuneOgsPageShift,        // ogs plan: log2 of the page size of the breadth-first chunk order
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -899,26 +899,39 @@ bool partition_rows(int32_t nrows, const int32_t* rs, std::vector<int32_t>& bloc
   return true;
 }
 
+// Checks run in parallel; a failure reports the lowest offending row or entry, so
+// the message does not depend on the thread schedule.
 static sp_status validate_csr(int32_t N, int32_t nrows, const int32_t* rs, const int32_t* ids,
                               const char* which, int32_t& maxRow) {
   if (nrows < 0) return fail(SP_ERR_INVALID_ARG, "ogs plan: negative row count (%s)", which);
   if (!rs) return fail(SP_ERR_INVALID_ARG, "ogs plan: null rowStarts (%s)", which);
   if (rs[0] != 0) return fail(SP_ERR_CSR, "ogs plan: rowStarts[0] != 0 (%s)", which);
+  int32_t bad = std::numeric_limits<int32_t>::max(), mx = maxRow;
+#pragma omp parallel for schedule(static) reduction(min : bad) reduction(max : mx)
   for (int32_t r = 0; r < nrows; ++r) {
     const int32_t len = rs[r + 1] - rs[r];
-    if (len < 0) return fail(SP_ERR_CSR, "ogs plan: rowStarts not monotone at %d (%s)", r, which);
-    if (len > kOgsMaxRowSize)
-      return fail(SP_ERR_SIZE,
-                  "Multiplicity of a global node in ogsOperator_t::setupRowBlocks is too large "
-                  "(row %d has %d > %d members, %s)",
-                  r, len, kOgsMaxRowSize, which);
-    maxRow = std::max(maxRow, len);
+    if (len < 0 || len > kOgsMaxRowSize)
+      bad = std::min(bad, r);
+    else
+      mx = std::max(mx, len);
   }
+  if (bad != std::numeric_limits<int32_t>::max()) {
+    const int32_t len = rs[bad + 1] - rs[bad];
+    if (len < 0)
+      return fail(SP_ERR_CSR, "ogs plan: rowStarts not monotone at %d (%s)", bad, which);
+    return fail(SP_ERR_SIZE,
+                "Multiplicity of a global node in ogsOperator_t::setupRowBlocks is too large "
+                "(row %d has %d > %d members, %s)",
+                bad, len, kOgsMaxRowSize, which);
+  }
+  maxRow = mx;
   const int32_t nnz = rs[nrows];
   if (nnz > 0 && !ids) return fail(SP_ERR_INVALID_ARG, "ogs plan: null colIds (%s)", which);
+#pragma omp parallel for schedule(static) reduction(min : bad)
   for (int32_t i = 0; i < nnz; ++i)
-    if (ids[i] < 0 || ids[i] >= N)
-      return fail(SP_ERR_CSR, "ogs plan: colIds[%d]=%d outside [0,%d) (%s)", i, ids[i], N, which);
+    if (ids[i] < 0 || ids[i] >= N) bad = std::min(bad, i);
+  if (bad != std::numeric_limits<int32_t>::max())
+    return fail(SP_ERR_CSR, "ogs plan: colIds[%d]=%d outside [0,%d) (%s)", bad, ids[bad], N, which);
   return SP_SUCCESS;
 }
 
@@ -978,24 +991,48 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     p->nnzN = p->rowStartsN[p->NrowsN];
     // every column at most once in T, and N's members of a row inside T's row
     std::vector<int32_t> rowOf(std::max(p->N, 1), -1);
+    int32_t dup = std::numeric_limits<int32_t>::max();
+    const int32_t* rsT = p->rowStartsT.data();
+    const int32_t* ciT = p->colIdsT.data();
+#pragma omp parallel for schedule(static) reduction(min : dup)
     for (int32_t r = 0; r < p->NrowsT; ++r)
-      for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) {
-        if (rowOf[p->colIdsT[i]] != -1)
-          return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", p->colIdsT[i]);
-        rowOf[p->colIdsT[i]] = r;
+      for (int32_t i = rsT[r]; i < rsT[r + 1]; ++i) {
+        int32_t prev;
+#pragma omp atomic capture
+        {
+          prev = rowOf[ciT[i]];
+          rowOf[ciT[i]] = r;
+        }
+        if (prev != -1) dup = std::min(dup, ciT[i]);
       }
+    if (dup != std::numeric_limits<int32_t>::max())
+      return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", dup);
+    int32_t badRow = std::numeric_limits<int32_t>::max();
+    const int32_t* rsN = p->rowStartsN.data();
+    const int32_t* ciN = p->colIdsN.data();
+#pragma omp parallel for schedule(static) reduction(min : badRow)
     for (int32_t r = 0; r < p->NrowsN; ++r)
-      for (int32_t i = p->rowStartsN[r]; i < p->rowStartsN[r + 1]; ++i)
-        if (rowOf[p->colIdsN[i]] != r)
-          return fail(SP_ERR_CSR, "ogs plan: N column %d of row %d is not in T row %d",
-                      p->colIdsN[i], r, r);
+      for (int32_t i = rsN[r]; i < rsN[r + 1]; ++i)
+        if (rowOf[ciN[i]] != r) badRow = std::min(badRow, r);
+    if (badRow != std::numeric_limits<int32_t>::max())
+      return fail(SP_ERR_CSR, "ogs plan: an N column of row %d is not in T row %d", badRow,
+                  badRow);
   } else {
     std::vector<uint8_t> seen(std::max(p->N, 1), 0);
+    int32_t dup = std::numeric_limits<int32_t>::max();
+    const int32_t* ciT = p->colIdsT.data();
+#pragma omp parallel for schedule(static) reduction(min : dup)
     for (int32_t i = 0; i < p->nnzT; ++i) {
-      if (seen[p->colIdsT[i]])
-        return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", p->colIdsT[i]);
-      seen[p->colIdsT[i]] = 1;
+      uint8_t prev;
+#pragma omp atomic capture
+      {
+        prev = seen[ciT[i]];
+        seen[ciT[i]] = 1;
+      }
+      if (prev) dup = std::min(dup, ciT[i]);
     }
+    if (dup != std::numeric_limits<int32_t>::max())
+      return fail(SP_ERR_CSR, "ogs plan: column %d appears in two rows", dup);
     p->NrowsN = std::min(p->NrowsN, p->NrowsT);
     p->rowStartsN.assign(p->rowStartsT.begin(), p->rowStartsT.begin() + p->NrowsN + 1);
     p->colIdsN.assign(p->colIdsT.begin(), p->colIdsT.begin() + p->rowStartsN[p->NrowsN]);
@@ -1032,13 +1069,15 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     p->own_blocks_n = true;
     if ((st = upload(blocksN, &p->d_blocksN, s))) return st;
   }
-  // warp chunks (only when every row fits one chunk)
+  // warp chunks (only when every row fits one chunk): T in the chosen order; N,
+  // whose rows hold at most one member after a unique setup, in row order
   p->chunk_order = (int32_t)tune(kTuneOgsOrder);
+  const int page_shift = (int)tune(kTuneOgsPageShift);
   std::vector<int32_t> chunksT, chunksN;
   if (build_chunks(p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), p->N, p->chunk_order,
-                   chunksT) &&
-      build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, p->chunk_order,
-                   chunksN)) {
+                   chunksT, page_shift) &&
+      build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, 0, chunksN,
+                   page_shift)) {
     p->nchunksT = (int32_t)(chunksT.size() / 2);
     p->nchunksN = (int32_t)(chunksN.size() / 2);
     // descriptors (r0, r1, g0, g1): the entry range rides along with the row range
@@ -1073,7 +1112,8 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     // T chunk entries in column order: the column-order scatter and gathers
     std::vector<int32_t> colS;
     std::vector<uint8_t> rowOf, e2s;
-    build_sorted(chunksT, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(),
+    build_sorted(chunksT, p->NrowsT, p->rowStartsT.data(),
+                 p->row_order == 1 ? rowsG.data() : nullptr,
                  p->row_order == 1 ? colIdsG.data() : p->colIdsT.data(), colS, rowOf, e2s);
     if ((st = upload(colS, &p->d_colIdsST, s))) return st;
     if ((st = upload(rowOf, &p->d_rowOfST, s))) return st;

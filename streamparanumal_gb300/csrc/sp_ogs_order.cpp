@@ -5,20 +5,22 @@
 // same results (each row is summed by one lane in CSR order), so the partition and
 // the chunk order are free to serve memory locality:
 //   order 0 (natural): chunks follow the row order;
-//   order 1 (bfs): rows are grouped by the 4 KiB page of local data holding their
-//     first member, pages are visited breadth-first over the "row joins pages"
-//     graph, and each page's rows are cut into chunks in that order.  Pages that
-//     share rows are then processed close together in time, so the data one chunk
-//     touches in a neighbouring page is usually still in L2 when that page's own
-//     chunks run -- whatever the element numbering in memory.
+//   order 1 (bfs): rows are grouped by the page (2^page_shift entries of local data,
+//     knob ogs.page_shift) holding their first member, pages are visited
+//     breadth-first over the "row joins pages" graph, and each page's rows are cut
+//     into chunks in that order.  Pages that share rows are then processed close
+//     together in time, so the data one chunk touches in a neighbouring page is
+//     usually still in L2 when that page's own chunks run -- whatever the element
+//     numbering in memory.  A page of about one element's nodes makes the visit a
+//     wavefront over the mesh.
+#include <parallel/algorithm>
+
 #include <algorithm>
 #include <vector>
 
 #include "sp_ogs_plan.h"
 
 namespace sp {
-
-static constexpr int kPageShift = 9;  // 512 entries per page
 
 static void cut_run(int32_t ra, int32_t rb, const int32_t* rs, std::vector<int32_t>& chunks) {
   int32_t c0 = ra;
@@ -35,52 +37,156 @@ static void cut_run(int32_t ra, int32_t rb, const int32_t* rs, std::vector<int32
   }
 }
 
+// Number of chunks cut_run makes of rows [ra, rb).
+static int32_t count_run(int32_t ra, int32_t rb, const int32_t* rs) {
+  int32_t n = 0, c0 = ra;
+  for (int32_t r = ra; r < rb; ++r)
+    if (rs[r + 1] - rs[c0] > kWarpChunkNnz || r - c0 >= kWarpChunkNnz) {
+      ++n;
+      c0 = r;
+    }
+  return n + (rb > c0 ? 1 : 0);
+}
+
+// Calls f(ra, rb) for each maximal run of consecutive rows in rows[a, b).
+template <typename F>
+static void for_runs(const int32_t* rows, int32_t a, int32_t b, F f) {
+  int32_t k = a;
+  while (k < b) {
+    const int32_t ra = rows[k];
+    int32_t rb = ra + 1;
+    ++k;
+    while (k < b && rows[k] == rb) {
+      ++rb;
+      ++k;
+    }
+    f(ra, rb);
+  }
+}
+
 bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols, int order,
-                  std::vector<int32_t>& chunks) {
+                  std::vector<int32_t>& chunks, int page_shift) {
   chunks.clear();
+  int32_t tooBig = 0;
+#pragma omp parallel for schedule(static) reduction(max : tooBig)
   for (int32_t r = 0; r < nrows; ++r)
-    if (rs[r + 1] - rs[r] > kWarpChunkNnz) return false;
+    if (rs[r + 1] - rs[r] > kWarpChunkNnz) tooBig = 1;
+  if (tooBig) return false;
   if (nrows == 0) return true;
   if (order == 0) {
     cut_run(0, nrows, rs, chunks);
     return true;
   }
-  const int32_t npages = (std::max(ncols, 1) + (1 << kPageShift) - 1) >> kPageShift;
-  // page of each row's first member; rows grouped by page (ascending row inside)
-  std::vector<int32_t> pcount(npages + 1, 0);
+  const int64_t npages64 = ((int64_t)std::max(ncols, 1) + (1LL << page_shift) - 1) >> page_shift;
+  const int32_t npages = (int32_t)npages64;
+  // page of each row's first member, and the rows grouped by page (ascending row
+  // inside).  Rows numbered by first appearance have non-decreasing pages, which
+  // makes the grouping a pass over the rows; otherwise (page, row) keys are sorted.
   std::vector<int32_t> rowPage(nrows, -1);
+  int32_t unordered = 0, nonEmpty = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nonEmpty)
   for (int32_t r = 0; r < nrows; ++r)
     if (rs[r + 1] > rs[r]) {
-      rowPage[r] = ci[rs[r]] >> kPageShift;
-      ++pcount[rowPage[r] + 1];
+      rowPage[r] = ci[rs[r]] >> page_shift;
+      ++nonEmpty;
     }
-  for (int32_t p = 0; p < npages; ++p) pcount[p + 1] += pcount[p];
-  std::vector<int32_t> pageRows(pcount[npages]);
-  {
-    std::vector<int32_t> fill(pcount.begin(), pcount.end() - 1);
+#pragma omp parallel for schedule(static) reduction(max : unordered)
+  for (int32_t r = 1; r < nrows; ++r)
+    if (rowPage[r] < 0 || rowPage[r - 1] < 0 || rowPage[r] < rowPage[r - 1]) unordered = 1;
+  std::vector<int32_t> pageRows(nonEmpty);
+  std::vector<int32_t> pstart(npages + 1, 0);  // rows of page p: pageRows[pstart[p], pstart[p+1])
+  if (!unordered) {
+#pragma omp parallel for schedule(static)
+    for (int32_t r = 0; r < nrows; ++r) {
+      pageRows[r] = r;
+      if (r == 0 || rowPage[r] != rowPage[r - 1])
+        for (int32_t q = (r == 0 ? 0 : rowPage[r - 1] + 1); q <= rowPage[r]; ++q) pstart[q] = r;
+    }
+    for (int32_t q = rowPage[nrows - 1] + 1; q <= npages; ++q) pstart[q] = nrows;
+  } else {
+    std::vector<int64_t> key;
+    key.reserve(nonEmpty);
     for (int32_t r = 0; r < nrows; ++r)
-      if (rowPage[r] >= 0) pageRows[fill[rowPage[r]]++] = r;
+      if (rowPage[r] >= 0) key.push_back(((int64_t)rowPage[r] << 32) | r);
+    __gnu_parallel::sort(key.begin(), key.end());
+    std::vector<int32_t> pcount(npages + 1, 0);
+    for (int32_t k = 0; k < nonEmpty; ++k) {
+      pageRows[k] = (int32_t)(key[k] & 0xffffffff);
+      ++pcount[(int32_t)(key[k] >> 32) + 1];
+    }
+    for (int32_t q = 0; q < npages; ++q) pstart[q + 1] = pstart[q] + pcount[q + 1];
   }
-  // undirected page graph: first page of a row -- page of each member
-  std::vector<int32_t> stamp(npages, -1);
-  std::vector<std::pair<int32_t, int32_t>> edges;
-  for (int32_t p = 0; p < npages; ++p)
-    for (int32_t k = pcount[p]; k < pcount[p + 1]; ++k) {
+  // forward edges (a row's first page -> the pages of its other members), unique per
+  // page: counted, then written
+  auto forward = [&](int32_t p, std::vector<int32_t>& tmp) {
+    tmp.clear();
+    for (int32_t k = pstart[p]; k < pstart[p + 1]; ++k) {
       const int32_t r = pageRows[k];
-      for (int32_t i = rs[r]; i < rs[r + 1]; ++i) {
-        const int32_t q = ci[i] >> kPageShift;
-        if (q != p && stamp[q] != p) {
-          stamp[q] = p;
-          edges.emplace_back(p, q);
-          edges.emplace_back(q, p);
-        }
+      for (int32_t i = rs[r] + 1; i < rs[r + 1]; ++i) {
+        const int32_t q = ci[i] >> page_shift;
+        if (q != p) tmp.push_back(q);
       }
     }
-  std::sort(edges.begin(), edges.end());
-  edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
-  std::vector<int32_t> adjStart(npages + 1, 0);
-  for (auto& e : edges) ++adjStart[e.first + 1];
-  for (int32_t p = 0; p < npages; ++p) adjStart[p + 1] += adjStart[p];
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+  };
+  std::vector<int64_t> fstart(npages + 1, 0);
+#pragma omp parallel
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 1024)
+    for (int32_t p = 0; p < npages; ++p) {
+      forward(p, tmp);
+      fstart[p + 1] = (int64_t)tmp.size();
+    }
+  }
+  for (int32_t p = 0; p < npages; ++p) fstart[p + 1] += fstart[p];
+  std::vector<int32_t> fwd(fstart[npages]);
+#pragma omp parallel
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 1024)
+    for (int32_t p = 0; p < npages; ++p) {
+      forward(p, tmp);
+      std::copy(tmp.begin(), tmp.end(), fwd.begin() + fstart[p]);
+    }
+  }
+  // undirected adjacency: forward lists plus their reverses, sorted and unique
+  std::vector<int64_t> adjStart(npages + 1, 0);
+  {
+    std::vector<int32_t> rev(npages, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < fstart[npages]; ++e) {
+#pragma omp atomic
+      ++rev[fwd[e]];
+    }
+    for (int32_t p = 0; p < npages; ++p)
+      adjStart[p + 1] = adjStart[p] + (fstart[p + 1] - fstart[p]) + rev[p];
+  }
+  std::vector<int32_t> adj(adjStart[npages]);
+  std::vector<int64_t> fill(npages);
+#pragma omp parallel for schedule(static)
+  for (int32_t p = 0; p < npages; ++p) {
+    std::copy(fwd.begin() + fstart[p], fwd.begin() + fstart[p + 1], adj.begin() + adjStart[p]);
+    fill[p] = adjStart[p] + (fstart[p + 1] - fstart[p]);
+  }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int32_t p = 0; p < npages; ++p)
+    for (int64_t e = fstart[p]; e < fstart[p + 1]; ++e) {
+      const int32_t q = fwd[e];
+      int64_t at;
+#pragma omp atomic capture
+      at = fill[q]++;
+      adj[at] = p;
+    }
+  std::vector<int64_t> adjEnd(npages);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int32_t p = 0; p < npages; ++p) {
+    int32_t* b = adj.data() + adjStart[p];
+    int32_t* e = adj.data() + adjStart[p + 1];
+    std::sort(b, e);
+    adjEnd[p] = std::unique(b, e) - adj.data();
+  }
   // breadth-first page order, restarting at the lowest unvisited page
   std::vector<uint8_t> seen(npages, 0);
   std::vector<int32_t> queue;
@@ -92,8 +198,8 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
     queue.push_back(start);
     while (head < queue.size()) {
       const int32_t p = queue[head++];
-      for (int32_t k = adjStart[p]; k < adjStart[p + 1]; ++k) {
-        const int32_t q = edges[k].second;
+      for (int64_t k = adjStart[p]; k < adjEnd[p]; ++k) {
+        const int32_t q = adj[k];
         if (!seen[q]) {
           seen[q] = 1;
           queue.push_back(q);
@@ -101,24 +207,38 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
       }
     }
   }
-  // chunks: each page's rows as maximal contiguous runs, in page visit order
-  for (int32_t p : queue) {
-    int32_t k = pcount[p];
-    while (k < pcount[p + 1]) {
-      int32_t ra = pageRows[k], rb = ra + 1;
-      ++k;
-      while (k < pcount[p + 1] && pageRows[k] == rb) {
-        ++rb;
-        ++k;
-      }
-      cut_run(ra, rb, rs, chunks);
+  // chunks: each page's rows as maximal consecutive runs, pages in visit order;
+  // counted per page, then cut in parallel into their places
+  std::vector<int64_t> cstart(npages + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int32_t k = 0; k < npages; ++k) {
+    const int32_t p = queue[k];
+    int64_t n = 0;
+    for_runs(pageRows.data(), pstart[p], pstart[p + 1],
+             [&](int32_t ra, int32_t rb) { n += count_run(ra, rb, rs); });
+    cstart[k + 1] = n;
+  }
+  for (int32_t k = 0; k < npages; ++k) cstart[k + 1] += cstart[k];
+  const int32_t nEmpty = nrows - nonEmpty;
+  chunks.resize(2 * (cstart[npages] + nEmpty));
+#pragma omp parallel
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 1024)
+    for (int32_t k = 0; k < npages; ++k) {
+      const int32_t p = queue[k];
+      tmp.clear();
+      for_runs(pageRows.data(), pstart[p], pstart[p + 1],
+               [&](int32_t ra, int32_t rb) { cut_run(ra, rb, rs, tmp); });
+      std::copy(tmp.begin(), tmp.end(), chunks.begin() + 2 * cstart[k]);
     }
   }
   // rows without members (possible in a caller-built CSR) still need a chunk
-  for (int32_t r = 0; r < nrows; ++r)
+  int64_t at = 2 * cstart[npages];
+  for (int32_t r = 0; r < nrows && nEmpty > 0; ++r)
     if (rowPage[r] < 0) {
-      chunks.push_back(r);
-      chunks.push_back(r + 1);
+      chunks[at++] = r;
+      chunks[at++] = r + 1;
     }
   return true;
 }
@@ -147,7 +267,7 @@ void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32
 }
 
 void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rs,
-                  const int32_t* ci, const int32_t* ciE, std::vector<int32_t>& colS,
+                  const int32_t* rowsG, const int32_t* ciE, std::vector<int32_t>& colS,
                   std::vector<uint8_t>& rowOf, std::vector<uint8_t>& e2s) {
   const int64_t nchunks = (int64_t)quads.size() / 4;
   const int32_t nnz = nrows > 0 ? rs[nrows] : 0;
@@ -157,19 +277,28 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
 #pragma omp parallel for schedule(dynamic, 256)
   for (int64_t c = 0; c < nchunks; ++c) {
     const int32_t r0 = quads[4 * c], r1 = quads[4 * c + 1], g0 = quads[4 * c + 2];
-    int64_t key[kWarpChunkNnz];  // column << 8 | row offset: sorts by column
-    int32_t n = 0;
-    for (int32_t r = r0; r < r1; ++r)
-      for (int32_t i = rs[r]; i < rs[r + 1]; ++i) key[n++] = ((int64_t)ci[i] << 8) | (r - r0);
-    std::sort(key, key + n);
-    int32_t* cs = colS.data() + g0;
-    for (int32_t j = 0; j < n; ++j) {
-      cs[j] = (int32_t)(key[j] >> 8);
-      rowOf[g0 + j] = (uint8_t)(key[j] & 0xFF);
+    const int32_t n = quads[4 * c + 3] - g0, nr = r1 - r0;
+    uint8_t rowOfE[kWarpChunkNnz];  // row offset of each entry of the row walk
+    if (rowsG) {
+      for (int32_t k = 0; k < nr; ++k) {
+        const int32_t a = rowsG[r0 + k] & 0xFFFF;
+        const int32_t b = (k + 1 < nr) ? (rowsG[r0 + k + 1] & 0xFFFF) : n;
+        for (int32_t e = a; e < b; ++e) rowOfE[e] = (uint8_t)(rowsG[r0 + k] >> 16);
+      }
+    } else {
+      for (int32_t r = r0; r < r1; ++r)
+        for (int32_t i = rs[r]; i < rs[r + 1]; ++i) rowOfE[i - g0] = (uint8_t)(r - r0);
     }
-    // every column appears once in a chunk, so its sorted position is unique
-    for (int32_t e = 0; e < n; ++e)
-      e2s[g0 + e] = (uint8_t)(std::lower_bound(cs, cs + n, ciE[g0 + e]) - cs);
+    // column << 8 | entry: sorts by column (every column appears once in a chunk)
+    int64_t key[kWarpChunkNnz];
+    for (int32_t e = 0; e < n; ++e) key[e] = ((int64_t)ciE[g0 + e] << 8) | e;
+    std::sort(key, key + n);
+    for (int32_t j = 0; j < n; ++j) {
+      const int32_t e = (int32_t)(key[j] & 0xFF);
+      colS[g0 + j] = (int32_t)(key[j] >> 8);
+      rowOf[g0 + j] = rowOfE[e];
+      e2s[g0 + e] = (uint8_t)j;
+    }
   }
 }
 

@@ -43,10 +43,11 @@ struct OgsOperatorDev {
 bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t>& blocks);
 
 // Cuts rows [0, nrows) into warp chunks, stored as (first row, end row) pairs in the
-// order they are scheduled: 0 = row order, 1 = breadth-first over 4 KiB pages of
-// local data.  Returns false when a row holds more than kWarpChunkNnz entries.
+// order they are scheduled: 0 = row order, 1 = breadth-first over pages of
+// 2^page_shift local entries.  Returns false when a row holds more than
+// kWarpChunkNnz entries.
 bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
-                  int order, std::vector<int32_t>& chunks);
+                  int order, std::vector<int32_t>& chunks, int page_shift);
 
 // Rows of every chunk regrouped by size.  `quads` holds the chunk descriptors
 // (r0, r1, g0, g1).  Inside chunk [r0, r1) the rows are reordered by member count,
@@ -64,13 +65,18 @@ void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32
 // data in address order.  For chunk (r0, r1, g0, g1): colIdsS[g0 + j] is the j-th
 // smallest column of the chunk and rowOfS[g0 + j] the offset from r0 of the row it
 // belongs to (a scatter writes v[colIdsS[j]] = gv[r0 + rowOfS[j]] with neighbouring
-// lanes on neighbouring addresses, and needs no row bounds).  `colIdsE` lists the
-// chunk's entries in the order the row bounds walk them (CSR order, or grouped by
-// size); e2s[g0 + e] is the sorted position of entry e of that order, so a gather
-// can load values in column order and still combine each row in CSR order.
+// lanes on neighbouring addresses, and needs no row bounds).  The row walk of the
+// gathers is CSR order (rowsG null, colIdsE = the CSR column ids) or grouped by
+// size (rowsG and colIdsE from build_grouped); e2s[g0 + e] is the sorted position
+// of entry e of that walk, so a gather can load values in column order and still
+// combine each row in CSR order.
 void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rowStarts,
-                  const int32_t* colIds, const int32_t* colIdsE, std::vector<int32_t>& colIdsS,
+                  const int32_t* rowsG, const int32_t* colIdsE, std::vector<int32_t>& colIdsS,
                   std::vector<uint8_t>& rowOfS, std::vector<uint8_t>& e2s);
+
+// Element slots of an nx*ny*nz box: slot[e] is where lexicographic element e is
+// stored (identity for perm_seed 0, else a seeded Fisher-Yates shuffle).
+std::vector<int32_t> box_slots(int64_t E, uint64_t perm_seed);
 
 }  // namespace sp
 

@@ -108,6 +108,28 @@ static void build_groups(int32_t N, const int64_t* ids, Groups& g) {
   }
 }
 
+// Element slots of a box (lexicographic element e = ex + ey*nx + ez*nx*ny is stored
+// at slot[e]): the identity, or a Fisher-Yates shuffle driven by SplitMix64 from
+// perm_seed.
+std::vector<int32_t> box_slots(int64_t E, uint64_t perm_seed) {
+  std::vector<int32_t> slot(E);
+  std::iota(slot.begin(), slot.end(), 0);
+  if (perm_seed != 0) {
+    uint64_t st = perm_seed;
+    auto splitmix = [&st]() {
+      uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+      return z ^ (z >> 31);
+    };
+    for (int64_t i = E - 1; i > 0; --i) {
+      const int64_t j = (int64_t)(splitmix() % (uint64_t)(i + 1));
+      std::swap(slot[i], slot[j]);
+    }
+  }
+  return slot;
+}
+
 }  // namespace sp
 
 using namespace sp;
@@ -232,22 +254,7 @@ sp_status sp_mesh_box_hex_ids(int32_t nx, int32_t ny, int32_t nz, int32_t p, uin
     return fail(SP_ERR_SIZE, "sp_mesh_box_hex_ids: %lld local nodes exceed int32", (long long)Ntot);
   const int64_t LX = (int64_t)nx * p + 1, LY = (int64_t)ny * p + 1, LZ = (int64_t)nz * p + 1;
 
-  // slot of each lexicographic element (e = ex + ey*nx + ez*nx*ny)
-  std::vector<int32_t> slot(E);
-  std::iota(slot.begin(), slot.end(), 0);
-  if (perm_seed != 0) {
-    uint64_t st = perm_seed;
-    auto splitmix = [&st]() {
-      uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
-      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-      return z ^ (z >> 31);
-    };
-    for (int64_t i = E - 1; i > 0; --i) {
-      const int64_t j = (int64_t)(splitmix() % (uint64_t)(i + 1));
-      std::swap(slot[i], slot[j]);
-    }
-  }
+  const std::vector<int32_t> slot = box_slots(E, perm_seed);
   // smallest local index on each lattice point
   std::vector<int32_t> minLocal((size_t)(LX * LY * LZ), 2147483647);
   for (int64_t e = 0; e < E; ++e) {

@@ -39,6 +39,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.kernel.gather", 0, 4, {2}},
     {"ogs.kernel.scatter", 0, 3, {3}},
     {"ogs.rows", 0, 1, {1}},
+    {"ogs.page_shift", 3, 16, {9}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

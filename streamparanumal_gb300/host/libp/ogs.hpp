@@ -39,6 +39,11 @@ class ogs_t {
   void Setup(const dlong _N, memory<hlong> ids, comm_t _comm, const Kind _kind,
              const Method method, const bool _unique, const bool verbose,
              platform_t& _platform);
+  // The same setup from ids already in device memory (grouped on the GPU by
+  // sp_ogs_setup_device; unique signs written back into o_ids).
+  void Setup(const dlong _N, deviceMemory<hlong> o_ids, comm_t _comm, const Kind _kind,
+             const Method method, const bool _unique, const bool verbose,
+             platform_t& _platform);
   void Free();
   sp_ogs_plan* plan() const { return plan_ ? plan_->p : nullptr; }
 
@@ -129,6 +134,7 @@ class ogs_t {
   };
   std::shared_ptr<planHolder> plan_;
   void need() const { LIBP_ABORT("ogs handle is not set up.", !plan_); }
+  void attach(std::shared_ptr<planHolder> holder, const timePoint_t start, const bool verbose);
 };
 
 }  // namespace ogs

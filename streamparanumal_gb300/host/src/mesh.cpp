@@ -46,13 +46,18 @@ void mesh_t::Setup(platform_t& _platform, settings_t& _settings, comm_t _comm) {
   NelementsGlobal = Nelements;
   const long long Nlocal = (long long)Nelements * Np;
   LIBP_ABORT("Local node count " << Nlocal << " exceeds dlong", Nlocal > 2147483647LL);
-  globalIds.malloc((size_t)Nlocal);
-  checkStatus(sp_mesh_box_hex_ids(nx, ny, nz, N, permSeed,
-                                  reinterpret_cast<int64_t*>(globalIds.ptr())),
+  // global ids generated and grouped on the device; the signed ids (one positive
+  // member per group) are then kept on the host as mesh_t::globalIds
+  deviceMemory<hlong> o_globalIds = platform.malloc<hlong>((size_t)Nlocal);
+  checkStatus(sp_mesh_box_hex_ids_device(nx, ny, nz, N, permSeed,
+                                         reinterpret_cast<int64_t*>(o_globalIds.ptr()),
+                                         (sp_stream_t)platform.stream()),
               "mesh_t::Setup");
   const bool verbose = settings.hasSetting("VERBOSE") && settings.compareSetting("VERBOSE", "TRUE");
-  ogs.Setup((dlong)Nlocal, globalIds, comm, ogs::Signed, ogs::Auto, /*unique=*/true, verbose,
+  ogs.Setup((dlong)Nlocal, o_globalIds, comm, ogs::Signed, ogs::Auto, /*unique=*/true, verbose,
             platform);
+  globalIds.malloc((size_t)Nlocal);
+  o_globalIds.copyTo(globalIds);
 }
 
 }  // namespace libp

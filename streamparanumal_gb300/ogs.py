@@ -57,22 +57,32 @@ class ogs_t:
         self.unique = False
 
     # ------------------------------------------------------------ setup
-    def Setup(self, N: int, ids: np.ndarray, comm=None, kind: int = Signed, method: int = Auto,
+    def Setup(self, N: int, ids, comm=None, kind: int = Signed, method: int = Auto,
               unique: bool = False, verbose: bool = False, platform=None, stream=None) -> None:
         """Group the local indices by |ids| (0 = ignored, negative = flagged).
 
-        With ``unique`` the signs of ``ids`` are rewritten in place so that every
-        group has one positive member, as ogsBase_t::Setup does
-        (libs/ogs/ogsSetup.cpp:145-147).  ``comm``/``method`` are accepted for
-        signature compatibility; one rank needs no exchange."""
+        ``ids`` is a contiguous int64 numpy array (host setup) or CUDA tensor (the
+        setup runs on the device, sp_ogs_setup_device; same plan).  With ``unique``
+        the signs of ``ids`` are rewritten in place so that every group has one
+        positive member, as ogsBase_t::Setup does (libs/ogs/ogsSetup.cpp:145-147).
+        ``comm``/``method`` are accepted for signature compatibility; one rank needs
+        no exchange."""
         self.Free()
-        if not isinstance(ids, np.ndarray) or ids.dtype != np.int64 or not ids.flags.c_contiguous:
-            raise TypeError("ids must be a contiguous numpy int64 array")
-        if ids.size < N:
-            raise ValueError("ids shorter than N")
         h = ctypes.c_void_p()
-        capi.call("sp_ogs_setup", N, capi.i64p(ids), kind, int(bool(unique)), _stream(stream),
-                  ctypes.byref(h))
+        if isinstance(ids, torch.Tensor):
+            if not ids.is_cuda or ids.dtype != torch.int64 or not ids.is_contiguous():
+                raise TypeError("device ids must be a contiguous CUDA int64 tensor")
+            if ids.numel() < N:
+                raise ValueError("ids shorter than N")
+            capi.call("sp_ogs_setup_device", N, ids.data_ptr(), kind, int(bool(unique)),
+                      _stream(stream), ctypes.byref(h))
+        else:
+            if not isinstance(ids, np.ndarray) or ids.dtype != np.int64 or not ids.flags.c_contiguous:
+                raise TypeError("ids must be a contiguous numpy int64 array or CUDA tensor")
+            if ids.size < N:
+                raise ValueError("ids shorter than N")
+            capi.call("sp_ogs_setup", N, capi.i64p(ids), kind, int(bool(unique)), _stream(stream),
+                      ctypes.byref(h))
         self._attach(h, kind, unique)
         if verbose:
             print(f"ogs Setup: {self.NgatherGlobal} gathered nodes, {self.info.NrowBlocksT} "
@@ -189,9 +199,16 @@ class ogs_t:
                   _stream(stream))
 
 
-def box_hex_ids(nx: int, ny: int, nz: int, p: int, perm_seed: int = 0) -> np.ndarray:
-    """Global ids of an nx*ny*nz hex box of degree p (see sp_mesh_box_hex_ids)."""
+def box_hex_ids(nx: int, ny: int, nz: int, p: int, perm_seed: int = 0,
+                device=None, stream=None):
+    """Global ids of an nx*ny*nz hex box of degree p (see sp_mesh_box_hex_ids): a
+    numpy array, or with ``device`` a CUDA tensor filled by the device kernel."""
     n = nx * ny * nz * (p + 1) ** 3
+    if device is not None:
+        ids = torch.empty(n, dtype=torch.int64, device=device)
+        capi.call("sp_mesh_box_hex_ids_device", nx, ny, nz, p, perm_seed, ids.data_ptr(),
+                  _stream(stream))
+        return ids
     ids = np.empty(n, dtype=np.int64)
     capi.call("sp_mesh_box_hex_ids", nx, ny, nz, p, perm_seed, capi.i64p(ids))
     return ids

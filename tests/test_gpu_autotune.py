@@ -15,12 +15,12 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
     try:
         res = autotune.tune_ogs(4, 3, perm_seed=5, reps=2)
         best = res["best"]
-        assert set(best) >= {"order", "rows", "kernel_gs", "kernel_gather", "kernel_scatter",
-                             "block_nnz"}
-        # grouped plans (2) x (4 + 3 + 4) kernels, the breadth-first CSR plan x
-        # (4 + 2 + 4), the row-order CSR plan with block kernels too (5 + 3 + 5), and
-        # block kernels at block_nnz 1024 (3)
-        assert len(res["candidates"]) == 22 + 10 + 13 + 3
+        assert set(best) >= {"order", "rows", "page_shift", "kernel_gs", "kernel_gather",
+                             "kernel_scatter", "block_nnz"}
+        # grouped plans (2, plus 64-entry pages at p = 3) x (4 + 3 + 4) kernels, the
+        # breadth-first CSR plan x (4 + 2 + 4), the row-order CSR plan with block
+        # kernels too (5 + 3 + 5), and block kernels at block_nnz 1024 (3)
+        assert len(res["candidates"]) == 33 + 10 + 13 + 3
         table = {}
         autotune.record(table, res)
         path = tmp_path / "t.json"

@@ -261,3 +261,30 @@ def test_variants_types_ops(cuda, orc, kernel, rows, dtype, op):
     finally:
         for k, v in old.items():
             capi.tune_set(k, v)
+
+
+@pytest.mark.parametrize("shift", [3, 6, 12])
+def test_page_sizes_of_breadth_first_order(cuda, orc, shift):
+    """Breadth-first chunk order over pages of 8, 64 and 4096 entries: the same bits."""
+    old = {k: capi.tune_get(k) for k in KNOBS + ("ogs.page_shift",)}
+    try:
+        set_variant(2, 1, 1)
+        capi.tune_set("ogs.page_shift", shift)
+        ids = O.box_hex_ids(5, 4, 6, 3, 31)
+        h, ref = make(orc, ids)
+        assert h.info.chunkOrder == 1 and h.info.NchunksT > 0
+        rs, ci = ref["rsT"], ref["ciT"]
+        q = orc.uniform(ids.size, 5)
+        gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+        dq = torch.from_numpy(q).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+        g = orc.uniform(rs.size - 1, 6)
+        dq = torch.zeros(ids.size, dtype=torch.float64, device="cuda")
+        h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)
+        np.testing.assert_array_equal(host(dq), orc.scatter(rs, ci, g, np.zeros(ids.size)))
+    finally:
+        for k, v in old.items():
+            capi.tune_set(k, v)
