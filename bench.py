@@ -713,10 +713,12 @@ def run_batch(args, local_rank: int) -> None:
         for i in range(args.batch_count):
             ex, ey, ez = (int(v) for v in rng.integers(2, args.batch_emax + 1, size=3))
             p = int(rng.integers(2, 10))
-            ids = O.box_hex_ids(ex, ey, ez, p, int(rng.integers(1, 1 << 30)))
+            ids = O.box_hex_ids(ex, ey, ez, p, int(rng.integers(1, 1 << 30)), device=dev,
+                                stream=stream)
+            n = ids.numel()
             h = O.ogs_t()
-            h.Setup(ids.size, ids, unique=True, stream=stream)
-            n = ids.size
+            h.Setup(n, ids, unique=True, stream=stream)
+            del ids
             v = {k: torch.rand(n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
                  for k in ("x", "r", "p", "Ap", "q")}
             v["rr"] = torch.zeros(1, dtype=torch.float64, device=dev)
@@ -728,33 +730,46 @@ def run_batch(args, local_rank: int) -> None:
     setup_s = time.time() - t0
     sc = kernels.ReduceScratch(dev)
     sptr = stream.cuda_stream
-
-    def per_instance():
-        for h, v, a in zip(plans, vecs, alphas):
-            capi.call("sp_cg_update_f64", v["x"].numel(), a, v["p"].data_ptr(), v["Ap"].data_ptr(),
-                      v["x"].data_ptr(), v["r"].data_ptr(), v["rr"].data_ptr(), sc.ptr, sptr)
-            capi.call("sp_ogs_gather_scatter", h._plan, capi.DOUBLE, capi.ADD, capi.SYM, 1,
-                      v["q"].data_ptr(), sptr)
-
-    b = batch.Batch(plans, [v["x"] for v in vecs], [v["r"] for v in vecs],
-                    [v["p"] for v in vecs], [v["Ap"] for v in vecs], [v["rr"] for v in vecs],
-                    [v["q"] for v in vecs], alphas, stream=stream)
-    with torch.cuda.stream(stream):
-        g_inst = batch.Graph(stream)
-        with g_inst:
-            per_instance()
-        g_batch = batch.Graph(stream)
-        with g_batch:
-            b.run(stream=stream)
     reps = max(3, min(args.steps, 20))
-    res = {"per_instance_launches": _time(per_instance, stream, reps),
-           "per_instance_graph": _time(lambda: g_inst.launch(), stream, reps),
-           "batched_persistent": _time(lambda: b.run(stream=stream), stream, reps),
-           "batched_graph": _time(lambda: g_batch.launch(), stream, reps)}
+
+    def time_forms(vs, f32: bool) -> dict:
+        """Per-instance launches, the same launches from one graph, the batched
+        persistent launch, and that launch from a graph."""
+        cg = "sp_cg_update_f32" if f32 else "sp_cg_update_f64"
+        ty = capi.FLOAT if f32 else capi.DOUBLE
+
+        def per_instance():
+            for h, v, a in zip(plans, vs, alphas):
+                capi.call(cg, v["x"].numel(), a, v["p"].data_ptr(), v["Ap"].data_ptr(),
+                          v["x"].data_ptr(), v["r"].data_ptr(), v["rr"].data_ptr(), sc.ptr, sptr)
+                capi.call("sp_ogs_gather_scatter", h._plan, ty, capi.ADD, capi.SYM, 1,
+                          v["q"].data_ptr(), sptr)
+
+        b = batch.Batch(plans, [v["x"] for v in vs], [v["r"] for v in vs], [v["p"] for v in vs],
+                        [v["Ap"] for v in vs], [v["rr"] for v in vs], [v["q"] for v in vs],
+                        alphas, stream=stream)
+        with torch.cuda.stream(stream):
+            g_inst = batch.Graph(stream)
+            with g_inst:
+                per_instance()
+            g_batch = batch.Graph(stream)
+            with g_batch:
+                b.run(stream=stream)
+        return {"per_instance_launches": _time(per_instance, stream, reps),
+                "per_instance_graph": _time(lambda: g_inst.launch(), stream, reps),
+                "batched_persistent": _time(lambda: b.run(stream=stream), stream, reps),
+                "batched_graph": _time(lambda: g_batch.launch(), stream, reps)}
+
+    res = time_forms(vecs, False)
+    vecs32 = [{k: (t if k == "rr" else t.float()) for k, t in v.items()} for v in vecs]
+    res32 = time_forms(vecs32, True)
     nodes = sum(x[4] for x in sizes)
     ng = sum(x[5] for x in sizes)
+    # CG: x, p, r, Ap read, x, r written; BS8: row starts, column ids, q read and written
     nbytes = 48 * nodes + (ng + len(sizes)) * 4 + nodes * 4 + 16 * nodes
+    nbytes32 = 24 * nodes + (ng + len(sizes)) * 4 + nodes * 4 + 8 * nodes
     per = {k: round(v / len(sizes) * 1e3, 3) for k, v in res.items()}  # us per instance
+    per32 = {k: round(v / len(sizes) * 1e3, 3) for k, v in res32.items()}
     line = {"metric": "batched CG update + BS8 per-instance time", "unit": "us/instance",
             "value": per["batched_graph"], "higher_is_better": False, "n_gpus": 1,
             "steps": reps, "dtype": "f64", "data": "synthetic (seeded)",
@@ -765,6 +780,13 @@ def run_batch(args, local_rank: int) -> None:
                                                        / res["batched_graph"], 3),
             "GBps_batched": round(nbytes / 1e6 / res["batched_persistent"], 1),
             "GBps_per_instance_launches": round(nbytes / 1e6 / res["per_instance_launches"], 1),
+            "fp32_storage": {
+                "per_instance_us": per32,
+                "speedup_batched_graph_vs_launches": round(res32["per_instance_launches"]
+                                                           / res32["batched_graph"], 3),
+                "GBps_batched": round(nbytes32 / 1e6 / res32["batched_persistent"], 1),
+                "useful_speedup_vs_fp64_batched": round(res["batched_persistent"]
+                                                        / res32["batched_persistent"], 3)},
             "launches": {"per_instance": 2 * len(sizes), "batched": 1},
             "setup_s": round(setup_s, 1)}
     print(json.dumps(line), flush=True)

@@ -65,14 +65,17 @@ void        sp_launch_count_reset(void);
  *    order-exact reductions;
  *  "ogs.block_nnz" (256..2048, default 2048): non-zeros per row block of plans
  *    created afterwards;
- *  "ogs.order" (0 row order, 1 breadth-first over pages of local data; default 1),
+ *  "ogs.order" (0 row order, 1 breadth-first over pages of local data, 2 rows
+ *    renumbered in that breadth-first order so that chunks are full; default 1),
  *    "ogs.page_shift" (3..16, default 9: pages of 2^9 entries) and "ogs.rows" (0
  *    CSR order, 1 rows grouped by size inside a chunk; default 1) for the warp
  *    chunks of plans created afterwards;
  *  "ogs.kernel" / "ogs.kernel.gather" / "ogs.kernel.scatter" (gather+scatter /
  *    gather / scatter): 0 block kernels, 1 warp-chunk kernels, 2 pipelined
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
- *    the column-order scatter, 4 column-order pipelined gathers; defaults 2, 2, 3.
+ *    the column-order scatter, 4 column-order pipelined gathers or the persistent
+ *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch
+ *    (gathers only); defaults 2, 2, 3.
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);
@@ -202,7 +205,7 @@ typedef struct {
   int64_t NgatherGlobal;
   int32_t NchunksT;   /* warp chunks of the T / N operators (0: block kernels only) */
   int32_t NchunksN;
-  int32_t chunkOrder; /* 0 row order, 1 breadth-first over pages of local data      */
+  int32_t chunkOrder; /* 0 row order, 1 breadth-first pages, 2 renumbered walk     */
   int32_t rowOrder;   /* T rows inside a chunk: 0 CSR order, 1 grouped by size      */
 } sp_ogs_info;
 
@@ -270,6 +273,13 @@ sp_status sp_batch_create(int32_t ninst, const sp_ogs_plan* const* plans, const 
                           double* const* x, double* const* r, const double* const* p,
                           const double* const* Ap, double* const* rdotr, double* const* q,
                           const double* alpha, sp_stream_t stream, sp_batch** out);
+/* FP32 storage: x, r, p, Ap, q in FP32 (x and r bit-identical to sp_cg_update_f32,
+ * q to the FP32 gather+scatter); r.r from compensated FP32 tile partials summed in
+ * FP64 into the FP64 rdotr[i]. */
+sp_status sp_batch_create_f32(int32_t ninst, const sp_ogs_plan* const* plans, const int64_t* n,
+                              float* const* x, float* const* r, const float* const* p,
+                              const float* const* Ap, double* const* rdotr, float* const* q,
+                              const double* alpha, sp_stream_t stream, sp_batch** out);
 sp_status sp_batch_run(const sp_batch* b, sp_stream_t stream);
 sp_status sp_batch_destroy(sp_batch* b);
 

@@ -32,14 +32,18 @@ DEFAULT_PAGE_SHIFT = 9
 
 def plan_configs(p: int) -> list[dict]:
     """PLAN_CONFIGS with the default 512-entry pages, plus breadth-first pages of
-    about one element ((p+1)^3 entries) when that size differs."""
+    about one element ((p+1)^3 entries) when that size differs, plus the
+    renumbered breadth-first walk over element-sized pages (chunk order 2)."""
     shift = max(3, ((p + 1) ** 3 - 1).bit_length())
     cfgs = [dict(c, page_shift=DEFAULT_PAGE_SHIFT) for c in PLAN_CONFIGS]
     if shift != DEFAULT_PAGE_SHIFT:
         cfgs.insert(1, {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": shift})
+    cfgs.insert(1, {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": shift})
     return cfgs
 KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
-           3: "warp-async-staged gathers / column-order scatter", 4: "column-order gathers"}
+           3: "warp-async-staged gathers / column-order scatter",
+           4: "column-order gathers / persistent prefetching column-order scatter",
+           5: "pipelined gathers with L2 prefetch of the next chunk"}
 OPS = (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs"))
 
 
@@ -71,13 +75,13 @@ def _set(cfg: dict) -> None:
 def _kernels(pc: dict, op: str) -> list[int]:
     """Kernel variants timed under one plan configuration: block kernels ignore the
     chunk order and row grouping, so they run once per block size; the column-order
-    scatter ignores the row grouping, so it runs under grouped plans only."""
+    scatters ignore the row grouping, so they run under grouped plans only."""
     ks = [0] if (pc["order"] == 0 and pc["rows"] == 0) else []
     if pc["block_nnz"] == 2048:
         if op == "BS7":
-            ks += [1, 2] + ([3] if pc["rows"] == 1 else [])
+            ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else [])
         else:
-            ks += [1, 2, 3, 4]
+            ks += [1, 2, 3, 4, 5]
     return ks
 
 

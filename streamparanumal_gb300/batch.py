@@ -32,9 +32,17 @@ class Batch:
         self._keep = (plans, x, r, p, Ap, rdotr, q)
         plan_ptrs = (ctypes.c_void_p * len(plans))(*[pl._plan for pl in plans])
         al = (ctypes.c_double * len(alpha))(*map(float, alpha))
-        capi.call("sp_batch_create", len(plans), plan_ptrs, capi.i64p(n), _ptrs(x), _ptrs(r),
-                  _ptrs(p), _ptrs(Ap), _ptrs(rdotr), _ptrs(q), al, _stream(stream),
-                  ctypes.byref(h))
+        dts = {t.dtype for group in (x, r, p, Ap, q) for t in group}
+        if dts == {torch.float64}:
+            fn = "sp_batch_create"
+        elif dts == {torch.float32}:
+            fn = "sp_batch_create_f32"  # FP32 storage, FP64 r.r
+        else:
+            raise TypeError("batch vectors must be all float64 or all float32")
+        if any(t.dtype != torch.float64 for t in rdotr):
+            raise TypeError("rdotr must be float64")
+        capi.call(fn, len(plans), plan_ptrs, capi.i64p(n), _ptrs(x), _ptrs(r), _ptrs(p),
+                  _ptrs(Ap), _ptrs(rdotr), _ptrs(q), al, _stream(stream), ctypes.byref(h))
         self._h = h
 
     def run(self, stream=None) -> None:

@@ -99,6 +99,8 @@ SIGNATURES = {
     "sp_ogs_gather_scatter": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P]),
     "sp_batch_create": (c_int32, [c_int32, _P, _I64P, _P, _P, _P, _P, _P, _P, _P, _P,
                                   POINTER(c_void_p)]),
+    "sp_batch_create_f32": (c_int32, [c_int32, _P, _I64P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                      POINTER(c_void_p)]),
     "sp_batch_run": (c_int32, [_P, _P]),
     "sp_batch_destroy": (c_int32, [_P]),
     "sp_mesh_box_hex_ids": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _I64P]),

@@ -289,6 +289,11 @@ __device__ __forceinline__ RowRef global_row(const int32_t* __restrict__ rs, int
   return RowRef{__ldg(rs + d.x + r) - d.z, __ldg(rs + d.x + r + 1) - d.z, r};
 }
 
+// Row of the operator for walk row w (the walk is renumbered only under chunk order 2).
+__device__ __forceinline__ int32_t op_row(const int32_t* __restrict__ perm, int32_t w) {
+  return perm ? __ldg(perm + w) : w;
+}
+
 template <typename T>
 __device__ __forceinline__ void warp_stage(const int32_t* __restrict__ ids, int32_t g0, int32_t gn,
                                            const T* v, T* sv, int lane,
@@ -338,7 +343,7 @@ template <typename T, int OP>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv,
-              int grouped) {
+              int grouped, const int32_t* __restrict__ perm) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
@@ -352,7 +357,7 @@ k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
     const RowRef q = staged_row(sm.rs[w], sm.ro[w], grouped, r);
-    gv[ch.x + q.row] = row_combine<T, OP>(sv, q.a, q.b);
+    gv[op_row(perm, ch.x + q.row)] = row_combine<T, OP>(sv, q.a, q.b);
   }
 }
 
@@ -360,7 +365,7 @@ template <typename T>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
                const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
-               int grouped) {
+               int grouped, const int32_t* __restrict__ perm) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
@@ -376,7 +381,7 @@ k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
   }
   for (int32_t r = lane; r < nr; r += 32) {
     const RowRef q = global_row(rs, grouped, ch, r);
-    const T x = gv[ch.x + q.row];
+    const T x = gv[op_row(perm, ch.x + q.row)];
     for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
   }
   __syncwarp();
@@ -399,10 +404,19 @@ __device__ __forceinline__ void load_cols(const int32_t* __restrict__ ids, int4 
   }
 }
 
-template <typename T, int OP, int MODE>  // MODE 0: gather+scatter (Sym), 1: gather
+// L2 prefetch of one element (a hint: no register, no scoreboard entry).
+__device__ __forceinline__ void prefetch_elem_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// PF = 1 (kernel 5): as soon as this chunk's values have landed, the next chunk's
+// values are prefetched into L2 from the column ids already in registers, so
+// they stream in while this chunk is combined and written back.
+template <typename T, int OP, int MODE, int PF = 0>  // MODE 0: gather+scatter (Sym), 1: gather
 __global__ void __launch_bounds__(kOgsThreads, kOgsPersistentCtas)
 k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
-              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped) {
+              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped,
+              const int32_t* __restrict__ perm) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
@@ -429,6 +443,12 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 #pragma unroll
     for (int u = 0; u < kOgsPerLane; ++u)
       if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+    if (PF) {
+      const int32_t gnn = dn.w - dn.z;
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u)
+        if (lane + 32 * u < gnn) prefetch_elem_l2(v + coln[u]);
+    }
     __syncwarp();
     for (int32_t r = lane; r < nr; r += 32) {
       const RowRef q = staged_row(srs, sro, grouped, r);
@@ -436,7 +456,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
       if (MODE == 0) {
         for (int32_t i = q.a; i < q.b; ++i) sv[i] = acc;
       } else {
-        gv[d.x + q.row] = acc;
+        gv[op_row(perm, d.x + q.row)] = acc;
       }
     }
     __syncwarp();
@@ -459,7 +479,7 @@ template <typename T>
 __global__ void __launch_bounds__(kOgsThreads, 4)
 k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
                const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
-               int grouped) {
+               int grouped, const int32_t* __restrict__ perm) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
@@ -478,7 +498,7 @@ k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     load_cols(ids, dn, lane, coln);
     for (int32_t r = lane; r < nr; r += 32) {
       const RowRef q = global_row(rs, grouped, d, r);
-      const T x = gv[d.x + q.row];
+      const T x = gv[op_row(perm, d.x + q.row)];
       for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
     }
     __syncwarp();
@@ -693,7 +713,8 @@ k_ogso_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads, kOgsScatterCtas)
 k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ colS,
-               const uint8_t* __restrict__ rowOf, const T* __restrict__ gv, T* __restrict__ v) {
+               const uint8_t* __restrict__ rowOf, const T* __restrict__ gv, T* __restrict__ v,
+               const int32_t* __restrict__ perm) {
   __shared__ T sres[kWarpsPerCta][kWarpChunkNnz];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c = blockIdx.x * kWarpsPerCta + w;
@@ -709,11 +730,66 @@ k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     col[u] = (i < sn) ? __ldg(colS + d.z + i) : 0;
     ro[u] = (i < sn) ? (int32_t)__ldg(rowOf + d.z + i) : 0;
   }
-  for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[d.x + r];
+  for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[op_row(perm, d.x + r)];
   __syncwarp();
 #pragma unroll
   for (int u = 0; u < kOgsPerLane; ++u)
     if (lane + 32 * u < sn) v[col[u]] = sr[ro[u]];
+}
+
+// Persistent column-order scatter (kernel 4 for scatters on T chunks): as kernel 3,
+// with each warp walking chunks c, c+W, ... and bulk-prefetching the next chunk's
+// three contiguous ranges (column ids, row offsets, gv slice) into L2 before
+// working on the current one.
+__device__ __forceinline__ void prefetch_range_l2(const void* base, int64_t first_byte,
+                                                  int64_t end_byte, int64_t limit_byte) {
+  const int64_t a = first_byte & ~(int64_t)15;
+  int64_t b = (end_byte + 15) & ~(int64_t)15;
+  const int64_t lim = limit_byte & ~(int64_t)15;
+  b = b < lim ? b : lim;
+  if (b > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)base + a),
+                 "r"((uint32_t)(b - a))
+                 : "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads, kOgsScatterCtas)
+k_ogssp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ colS,
+                const uint8_t* __restrict__ rowOf, const T* __restrict__ gv, T* __restrict__ v,
+                int64_t nnz, int64_t nrows) {
+  __shared__ T sres[kWarpsPerCta][kWarpChunkNnz];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  T* sr = sres[w];
+  while (c < nchunks) {
+    const int4 d = __ldg(chunks + c);
+    if (c + W < nchunks && lane < 3) {
+      const int4 e = __ldg(chunks + c + W);
+      if (lane == 0) prefetch_range_l2(colS, 4LL * e.z, 4LL * e.w, 4LL * nnz);
+      if (lane == 1) prefetch_range_l2(rowOf, e.z, e.w, nnz);
+      if (lane == 2)
+        prefetch_range_l2(gv, (int64_t)sizeof(T) * e.x, (int64_t)sizeof(T) * e.y,
+                          (int64_t)sizeof(T) * nrows);
+    }
+    const int32_t nr = d.y - d.x, sn = d.w - d.z;
+    int32_t col[kOgsPerLane];
+    int32_t ro[kOgsPerLane];
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u) {
+      const int i = lane + 32 * u;
+      col[u] = (i < sn) ? __ldg(colS + d.z + i) : 0;
+      ro[u] = (i < sn) ? (int32_t)__ldg(rowOf + d.z + i) : 0;
+    }
+    for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[d.x + r];
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < sn) v[col[u]] = sr[ro[u]];
+    __syncwarp();  // sres is refilled by the next chunk
+    c += W;
+  }
 }
 
 static inline unsigned persistent_grid(int32_t nchunks, int ctas_per_sm = 4) {
@@ -729,9 +805,10 @@ static inline unsigned warp_grid(int32_t nchunks) {
 // Kernel variant of an operation (knobs ogs.kernel / ogs.kernel.gather /
 // ogs.kernel.scatter): 0 block kernels, 1 warp chunks, 2 pipelined warp chunks,
 // 3 asynchronously staged warp chunks for the gathers and column-order warp chunks
-// for the scatter, 4 column-order pipelined gathers.  Launches through the N
-// operator take the pipelined kernels for the column-order variants.  The warp
-// variants need k == 1 and a plan with chunks.
+// for the scatter, 4 column-order pipelined gathers and the persistent
+// column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch of
+// the next chunk.  Launches through the N operator take the pipelined kernels for
+// the column-order variants.  The warp variants need k == 1 and a plan with chunks.
 static inline int variant(TuneKey key, int K, int32_t nchunks) {
   return (K == 1 && nchunks > 0) ? (int)tune(key) : 0;
 }
@@ -746,23 +823,32 @@ struct ChunkArgs {
   int grouped;
   const int32_t* colS;  // column-order entries (T chunks only, else null)
   const uint8_t* e2s;
+  const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
+  const int32_t* rs = p->d_walkRsT ? p->d_walkRsT : p->d_rowStartsT;
+  const int32_t* ci = p->d_walkCiT ? p->d_walkCiT : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
-                   g ? p->d_rowsGT : p->d_rowStartsT, g ? p->d_colIdsGT : p->d_colIdsT, g ? 1 : 0,
-                   p->d_colIdsST, p->d_e2sT};
+                   g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
+                   p->d_colIdsST, p->d_e2sT, p->d_permT};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-                   p->d_colIdsN, 0, nullptr, nullptr};
+                   p->d_colIdsN, 0, nullptr, nullptr, nullptr};
 }
 
 // ------------------------------------------------------------------ dispatch
 
 template <typename T, int OP, int MODE>
 static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaStream_t s) {
-  if (kv == 4 && a.e2s) {
+  // a gather through a renumbered walk writes gv through perm: kernels 1, 2, 5 do
+  if (MODE == 1 && a.perm && (kv == 3 || kv == 4)) kv = 2;
+  if (kv == 5) {
+    k_ogsp_gather<T, OP, MODE, 1><<<persistent_grid(a.nchunks, kOgsPersistentCtas), kOgsThreads,
+                                    0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped,
+                                            a.perm);
+  } else if (kv == 4 && a.e2s) {
     k_ogso_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.colS, a.e2s, v, gv, a.grouped);
   } else if (kv == 3) {
@@ -770,14 +856,14 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
         a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
   } else if (kv >= 2) {
     k_ogsp_gather<T, OP, MODE><<<persistent_grid(a.nchunks, kOgsPersistentCtas), kOgsThreads,
-                                 0, s>>>(
-        a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
+                                 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped,
+                                         a.perm);
   } else if (MODE == 0) {
     k_ogsw_gs_sym<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
                                                                      a.ids, v, a.grouped);
   } else {
-    k_ogsw_gather<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
-                                                                     a.ids, v, gv, a.grouped);
+    k_ogsw_gather<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
+        a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, a.perm);
   }
 }
 
@@ -825,18 +911,23 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
                            cudaStream_t s) {
   const bool useN = (trans == SP_TRANS);
   const int kv = variant(kTuneOgsKernelScatter, K, useN ? p->nchunksN : p->nchunksT);
-  if (kv == 3 && !useN && p->d_colIdsST) {
+  // the persistent prefetching scatter reads gv slices directly: not through perm
+  if (kv == 4 && !useN && p->d_colIdsST && !p->d_permT) {
+    k_ogssp_scatter<T><<<persistent_grid(p->nchunksT, kOgsScatterCtas), kOgsThreads, 0, s>>>(
+        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv,
+        v, (int64_t)p->nnzT, (int64_t)p->NrowsT);
+  } else if (kv >= 3 && !useN && p->d_colIdsST) {
     k_ogss_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv,
-        v);
+        v, p->d_permT);
   } else if (kv > 0) {
     const ChunkArgs a = useN ? chunks_n(p) : chunks_t(p);
     if (kv >= 2)
       k_ogsp_scatter<T><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
-          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped);
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, a.perm);
     else
-      k_ogsw_scatter<T><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
-                                                                     a.ids, gv, v, a.grouped);
+      k_ogsw_scatter<T><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, a.perm);
   } else if (useN) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_scatter<T><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
@@ -953,6 +1044,10 @@ static void free_plan_device(sp_ogs_plan* p) {
   if (p->d_colIdsST) cudaFree(p->d_colIdsST);
   if (p->d_rowOfST) cudaFree(p->d_rowOfST);
   if (p->d_e2sT) cudaFree(p->d_e2sT);
+  if (p->d_walkRsT) cudaFree(p->d_walkRsT);
+  if (p->d_walkCiT) cudaFree(p->d_walkCiT);
+  if (p->d_permT) cudaFree(p->d_permT);
+  p->d_walkRsT = p->d_walkCiT = p->d_permT = nullptr;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1070,18 +1165,47 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(blocksN, &p->d_blocksN, s))) return st;
   }
   // warp chunks (only when every row fits one chunk): T in the chosen order; N,
-  // whose rows hold at most one member after a unique setup, in row order
+  // whose rows hold at most one member after a unique setup, in row order.  Order 2
+  // walks a copy of T whose rows are renumbered in breadth-first page order (the
+  // rows of each page in turn), so chunks are full and follow the mesh whatever the
+  // element numbering; perm maps a walk row back to its row of T.
   p->chunk_order = (int32_t)tune(kTuneOgsOrder);
   const int page_shift = (int)tune(kTuneOgsPageShift);
+  const bool renumber = p->chunk_order == 2;
+  std::vector<int32_t> walkRs, walkCi, perm;
+  const int32_t* wrs = p->rowStartsT.data();
+  const int32_t* wci = p->colIdsT.data();
   std::vector<int32_t> chunksT, chunksN;
-  if (build_chunks(p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), p->N, p->chunk_order,
-                   chunksT, page_shift) &&
-      build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, 0, chunksN,
-                   page_shift)) {
+  bool fits = true;
+  if (renumber) {
+    int32_t tooBig = 0;
+#pragma omp parallel for schedule(static) reduction(max : tooBig)
+    for (int32_t r = 0; r < p->NrowsT; ++r)
+      if (p->rowStartsT[r + 1] - p->rowStartsT[r] > kWarpChunkNnz) tooBig = 1;
+    fits = !tooBig;
+    if (fits) {
+      bfs_row_sequence(p->NrowsT, wrs, wci, p->N, page_shift, perm);
+      walkRs.assign((size_t)p->NrowsT + 1, 0);
+      for (int32_t k = 0; k < p->NrowsT; ++k)
+        walkRs[k + 1] = walkRs[k] + (p->rowStartsT[perm[k] + 1] - p->rowStartsT[perm[k]]);
+      walkCi.resize(p->nnzT);
+#pragma omp parallel for schedule(static)
+      for (int32_t k = 0; k < p->NrowsT; ++k)
+        std::copy(p->colIdsT.begin() + p->rowStartsT[perm[k]],
+                  p->colIdsT.begin() + p->rowStartsT[perm[k] + 1], walkCi.begin() + walkRs[k]);
+      wrs = walkRs.data();
+      wci = walkCi.data();
+      fits = build_chunks(p->NrowsT, wrs, wci, p->N, 0, chunksT, page_shift);
+    }
+  } else {
+    fits = build_chunks(p->NrowsT, wrs, wci, p->N, p->chunk_order, chunksT, page_shift);
+  }
+  if (fits && build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, 0, chunksN,
+                           page_shift)) {
     p->nchunksT = (int32_t)(chunksT.size() / 2);
     p->nchunksN = (int32_t)(chunksN.size() / 2);
     // descriptors (r0, r1, g0, g1): the entry range rides along with the row range
-    auto quads = [](const std::vector<int32_t>& pairs, const std::vector<int32_t>& rs) {
+    auto quads = [](const std::vector<int32_t>& pairs, const int32_t* rs) {
       std::vector<int32_t> q(pairs.size() * 2);
       for (size_t c = 0; c < pairs.size() / 2; ++c) {
         q[4 * c + 0] = pairs[2 * c];
@@ -1091,9 +1215,9 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       }
       return q;
     };
-    const bool same = (chunksN == chunksT);
-    chunksT = quads(chunksT, p->rowStartsT);
-    chunksN = same ? chunksT : quads(chunksN, p->rowStartsN);
+    const bool same = !renumber && (chunksN == chunksT);
+    chunksT = quads(chunksT, wrs);
+    chunksN = same ? chunksT : quads(chunksN, p->rowStartsN.data());
     if ((st = upload(chunksT, &p->d_chunksT, s))) return st;
     if (same) {
       p->d_chunksN = p->d_chunksT;
@@ -1101,10 +1225,15 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       p->own_chunks_n = true;
       if ((st = upload(chunksN, &p->d_chunksN, s))) return st;
     }
+    if (renumber) {
+      if ((st = upload(walkRs, &p->d_walkRsT, s))) return st;
+      if ((st = upload(walkCi, &p->d_walkCiT, s))) return st;
+      if ((st = upload(perm, &p->d_permT, s))) return st;
+    }
     // T rows grouped by size inside each chunk (the N operator keeps CSR order)
     std::vector<int32_t> rowsG, colIdsG;
     if (tune(kTuneOgsRows) == 1 && p->nchunksT > 0) {
-      build_grouped(chunksT, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), rowsG, colIdsG);
+      build_grouped(chunksT, p->NrowsT, wrs, wci, rowsG, colIdsG);
       if ((st = upload(rowsG, &p->d_rowsGT, s))) return st;
       if ((st = upload(colIdsG, &p->d_colIdsGT, s))) return st;
       p->row_order = 1;
@@ -1112,13 +1241,14 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     // T chunk entries in column order: the column-order scatter and gathers
     std::vector<int32_t> colS;
     std::vector<uint8_t> rowOf, e2s;
-    build_sorted(chunksT, p->NrowsT, p->rowStartsT.data(),
-                 p->row_order == 1 ? rowsG.data() : nullptr,
-                 p->row_order == 1 ? colIdsG.data() : p->colIdsT.data(), colS, rowOf, e2s);
+    build_sorted(chunksT, p->NrowsT, wrs, p->row_order == 1 ? rowsG.data() : nullptr,
+                 p->row_order == 1 ? colIdsG.data() : wci, colS, rowOf, e2s);
     if ((st = upload(colS, &p->d_colIdsST, s))) return st;
     if ((st = upload(rowOf, &p->d_rowOfST, s))) return st;
     if ((st = upload(e2s, &p->d_e2sT, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+  } else {
+    p->nchunksT = p->nchunksN = 0;
   }
   SP_CUDA_TRY(cudaStreamSynchronize(s));
   return SP_SUCCESS;

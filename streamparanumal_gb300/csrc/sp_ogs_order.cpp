@@ -64,25 +64,26 @@ static void for_runs(const int32_t* rows, int32_t a, int32_t b, F f) {
   }
 }
 
-bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols, int order,
-                  std::vector<int32_t>& chunks, int page_shift) {
-  chunks.clear();
-  int32_t tooBig = 0;
-#pragma omp parallel for schedule(static) reduction(max : tooBig)
-  for (int32_t r = 0; r < nrows; ++r)
-    if (rs[r + 1] - rs[r] > kWarpChunkNnz) tooBig = 1;
-  if (tooBig) return false;
-  if (nrows == 0) return true;
-  if (order == 0) {
-    cut_run(0, nrows, rs, chunks);
-    return true;
-  }
+// Pages of local data (2^page_shift entries) visited breadth-first over the "row
+// joins pages" graph, restarting at the lowest unvisited page.
+struct PageOrder {
+  int32_t npages = 0, nonEmpty = 0;
+  std::vector<int32_t> rowPage;   // page of each row's first member, -1 if empty
+  std::vector<int32_t> pageRows;  // rows grouped by page, ascending inside
+  std::vector<int32_t> pstart;    // rows of page p: pageRows[pstart[p], pstart[p+1])
+  std::vector<int32_t> queue;     // pages in visit order
+};
+
+static void page_order(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols,
+                       int page_shift, PageOrder& po) {
   const int64_t npages64 = ((int64_t)std::max(ncols, 1) + (1LL << page_shift) - 1) >> page_shift;
   const int32_t npages = (int32_t)npages64;
+  po.npages = npages;
   // page of each row's first member, and the rows grouped by page (ascending row
   // inside).  Rows numbered by first appearance have non-decreasing pages, which
   // makes the grouping a pass over the rows; otherwise (page, row) keys are sorted.
-  std::vector<int32_t> rowPage(nrows, -1);
+  std::vector<int32_t>& rowPage = po.rowPage;
+  rowPage.assign(nrows, -1);
   int32_t unordered = 0, nonEmpty = 0;
 #pragma omp parallel for schedule(static) reduction(+ : nonEmpty)
   for (int32_t r = 0; r < nrows; ++r)
@@ -93,8 +94,11 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
 #pragma omp parallel for schedule(static) reduction(max : unordered)
   for (int32_t r = 1; r < nrows; ++r)
     if (rowPage[r] < 0 || rowPage[r - 1] < 0 || rowPage[r] < rowPage[r - 1]) unordered = 1;
-  std::vector<int32_t> pageRows(nonEmpty);
-  std::vector<int32_t> pstart(npages + 1, 0);  // rows of page p: pageRows[pstart[p], pstart[p+1])
+  po.nonEmpty = nonEmpty;
+  std::vector<int32_t>& pageRows = po.pageRows;
+  pageRows.assign(nonEmpty, 0);
+  std::vector<int32_t>& pstart = po.pstart;
+  pstart.assign(npages + 1, 0);
   if (!unordered) {
 #pragma omp parallel for schedule(static)
     for (int32_t r = 0; r < nrows; ++r) {
@@ -189,7 +193,8 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
   }
   // breadth-first page order, restarting at the lowest unvisited page
   std::vector<uint8_t> seen(npages, 0);
-  std::vector<int32_t> queue;
+  std::vector<int32_t>& queue = po.queue;
+  queue.clear();
   queue.reserve(npages);
   for (int32_t start = 0; start < npages; ++start) {
     if (seen[start]) continue;
@@ -207,6 +212,28 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
       }
     }
   }
+}
+
+bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols, int order,
+                  std::vector<int32_t>& chunks, int page_shift) {
+  chunks.clear();
+  int32_t tooBig = 0;
+#pragma omp parallel for schedule(static) reduction(max : tooBig)
+  for (int32_t r = 0; r < nrows; ++r)
+    if (rs[r + 1] - rs[r] > kWarpChunkNnz) tooBig = 1;
+  if (tooBig) return false;
+  if (nrows == 0) return true;
+  if (order == 0) {
+    cut_run(0, nrows, rs, chunks);
+    return true;
+  }
+  PageOrder po;
+  page_order(nrows, rs, ci, ncols, page_shift, po);
+  const int32_t npages = po.npages, nonEmpty = po.nonEmpty;
+  const std::vector<int32_t>& rowPage = po.rowPage;
+  const std::vector<int32_t>& pageRows = po.pageRows;
+  const std::vector<int32_t>& pstart = po.pstart;
+  const std::vector<int32_t>& queue = po.queue;
   // chunks: each page's rows as maximal consecutive runs, pages in visit order;
   // counted per page, then cut in parallel into their places
   std::vector<int64_t> cstart(npages + 1, 0);
@@ -241,6 +268,29 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
       chunks[at++] = r + 1;
     }
   return true;
+}
+
+void bfs_row_sequence(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols,
+                      int page_shift, std::vector<int32_t>& seq) {
+  seq.clear();
+  if (nrows == 0) return;
+  PageOrder po;
+  page_order(nrows, rs, ci, ncols, page_shift, po);
+  seq.resize(nrows);
+  std::vector<int64_t> at(po.npages + 1, 0);
+  for (int32_t k = 0; k < po.npages; ++k) {
+    const int32_t p = po.queue[k];
+    at[k + 1] = at[k] + (po.pstart[p + 1] - po.pstart[p]);
+  }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int32_t k = 0; k < po.npages; ++k) {
+    const int32_t p = po.queue[k];
+    std::copy(po.pageRows.begin() + po.pstart[p], po.pageRows.begin() + po.pstart[p + 1],
+              seq.begin() + at[k]);
+  }
+  int64_t n = at[po.npages];
+  for (int32_t r = 0; r < nrows && n < nrows; ++r)
+    if (po.rowPage[r] < 0) seq[n++] = r;
 }
 
 void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rs,

@@ -49,6 +49,11 @@ bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t
 bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
                   int order, std::vector<int32_t>& chunks, int page_shift);
 
+// All rows in breadth-first page order: each page's rows (ascending) as the pages
+// are visited, then rows without members.  seq[k] = the k-th row of the walk.
+void bfs_row_sequence(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds,
+                      int32_t ncols, int page_shift, std::vector<int32_t>& seq);
+
 // Rows of every chunk regrouped by size.  `quads` holds the chunk descriptors
 // (r0, r1, g0, g1).  Inside chunk [r0, r1) the rows are reordered by member count,
 // largest first (ties in row order), and their members are laid out in that order
@@ -110,6 +115,11 @@ struct sp_ogs_plan {
   int32_t* d_rowsGT = nullptr;       // NrowsT packed (start offset | row offset << 16)
   int32_t* d_colIdsGT = nullptr;     // nnzT
   int32_t row_order = 0;             // 1 when d_rowsGT / d_colIdsGT are in use
+  // order 2: T rows renumbered in breadth-first page order (the walk the warp
+  // kernels take), and each walk row's row of T; null otherwise (the walk is T)
+  int32_t* d_walkRsT = nullptr;      // NrowsT + 1
+  int32_t* d_walkCiT = nullptr;      // nnzT
+  int32_t* d_permT = nullptr;        // NrowsT
   // T chunk entries in column order (build_sorted), for the column-order scatter
   int32_t* d_colIdsST = nullptr;     // nnzT
   uint8_t* d_rowOfST = nullptr;      // nnzT

@@ -33,11 +33,11 @@ struct TuneEntry {
 static TuneEntry g_tune[kTuneCount] = {
     {"reduce.prefetch_chunks", -1, 64, {-1}},
     {"ogs.block_nnz", 256, 2048, {2048}},
-    {"ogs.kernel", 0, 4, {2}},
-    {"ogs.order", 0, 1, {1}},
+    {"ogs.kernel", 0, 5, {2}},
+    {"ogs.order", 0, 2, {1}},
     {"reduce.rolling", 0, 1, {1}},
-    {"ogs.kernel.gather", 0, 4, {2}},
-    {"ogs.kernel.scatter", 0, 3, {3}},
+    {"ogs.kernel.gather", 0, 5, {2}},
+    {"ogs.kernel.scatter", 0, 4, {3}},
     {"ogs.rows", 0, 1, {1}},
     {"ogs.page_shift", 3, 16, {9}},
 };

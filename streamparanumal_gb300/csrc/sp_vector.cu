@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "sp_internal.h"
+#include "sp_compensated.cuh"
 
 namespace sp {
 
@@ -529,23 +530,6 @@ __device__ __forceinline__ void finish_ticket(double block_val, RedScratch sc, d
     out[0] = r;
     *sc.ticket = 0u;  // leave the scratch zeroed for the next call
   }
-}
-
-// Error-free transformation a + b = s + e (Knuth TwoSum), FP32.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// Compensated FP32 accumulation of a product (Ogita-Rump-Oishi Dot2 step).
-__device__ __forceinline__ void dot2_step(float a, float b, float& s, float& c) {
-  const float p = a * b;
-  const float pe = fmaf(a, b, -p);
-  float t, e;
-  two_sum(s, p, t, e);
-  s = t;
-  c += e + pe;
 }
 
 template <int U>

@@ -17,10 +17,11 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
         best = res["best"]
         assert set(best) >= {"order", "rows", "page_shift", "kernel_gs", "kernel_gather",
                              "kernel_scatter", "block_nnz"}
-        # grouped plans (2, plus 64-entry pages at p = 3) x (4 + 3 + 4) kernels, the
-        # breadth-first CSR plan x (4 + 2 + 4), the row-order CSR plan with block
-        # kernels too (5 + 3 + 5), and block kernels at block_nnz 1024 (3)
-        assert len(res["candidates"]) == 33 + 10 + 13 + 3
+        # grouped plans (2, plus 64-entry pages at p = 3, plus the renumbered walk) x
+        # (5 + 4 + 5) kernels, the breadth-first CSR plan x (5 + 2 + 5), the row-order
+        # CSR plan with block kernels too (6 + 3 + 6), and block kernels at
+        # block_nnz 1024 (3)
+        assert len(res["candidates"]) == 56 + 12 + 15 + 3
         table = {}
         autotune.record(table, res)
         path = tmp_path / "t.json"

@@ -70,3 +70,65 @@ def test_batch_graph_replay_and_repeat(cuda, orc):
             g.launch()
     torch.cuda.synchronize()
     assert [t.item() for t in rdotr] == first  # tickets were reset; same order, same bits
+
+
+def test_batch_fp32_storage_matches_single_instance_calls(cuda, orc):
+    """FP32 storage: x, r and q bit-identical to the FP32 one-instance calls; r.r
+    (compensated FP32 partials, FP64 finish) within 1e-12 of the exact sum of the
+    FP32 r values' squares."""
+    inst = [(h, {k: t.float() for k, t in v.items()}, a) for h, v, a in instances(orc, 6, 29)]
+    ref = []
+    sc = K.ReduceScratch()
+    for h, v, alpha in inst:
+        x, r, q = v["x"].clone(), v["r"].clone(), v["q"].clone()
+        rr = torch.zeros(1, dtype=torch.float64, device="cuda")
+        K.cg_update(alpha, v["p"], v["Ap"], x, r, rr, sc)
+        h.GatherScatter(q, 1, O.Add, O.Sym)
+        ref.append((x, r, q))
+    rdotr = [torch.zeros(1, dtype=torch.float64, device="cuda") for _ in inst]
+    b = B.Batch([h for h, _, _ in inst], [v["x"] for _, v, _ in inst],
+                [v["r"] for _, v, _ in inst], [v["p"] for _, v, _ in inst],
+                [v["Ap"] for _, v, _ in inst], rdotr, [v["q"] for _, v, _ in inst],
+                [a for _, _, a in inst])
+    b.run()
+    torch.cuda.synchronize()
+    for (h, v, _), (x, r, q), rd in zip(inst, ref, rdotr):
+        assert torch.equal(v["x"], x) and torch.equal(v["r"], r) and torch.equal(v["q"], q)
+        exact = float(np.sum(r.cpu().numpy().astype(np.float64) ** 2))
+        assert abs(rd.item() - exact) <= 1e-12 * exact
+
+
+def test_batch_rejects_mixed_types(cuda, orc):
+    (h, v, a), = instances(orc, 1, 5)
+    rd = [torch.zeros(1, dtype=torch.float64, device="cuda")]
+    with pytest.raises(TypeError):
+        B.Batch([h], [v["x"].float()], [v["r"]], [v["p"]], [v["Ap"]], rd, [v["q"]], [a])
+
+
+@pytest.mark.parametrize("order,rows", [(2, 0), (2, 1), (0, 0)])
+def test_batch_with_every_chunk_walk(cuda, orc, order, rows):
+    """Plans whose chunks walk renumbered, grouped or plain rows: the batch gives the
+    one-instance bits."""
+    from streamparanumal_gb300 import capi
+    old = {k: capi.tune_get(k) for k in ("ogs.order", "ogs.rows")}
+    try:
+        capi.tune_set("ogs.order", order)
+        capi.tune_set("ogs.rows", rows)
+        inst = instances(orc, 4, 41)
+    finally:
+        for k, v in old.items():
+            capi.tune_set(k, v)
+    ref = []
+    for h, v, alpha in inst:
+        q = v["q"].clone()
+        h.GatherScatter(q, 1, O.Add, O.Sym)
+        ref.append(q)
+    rdotr = [torch.zeros(1, dtype=torch.float64, device="cuda") for _ in inst]
+    b = B.Batch([h for h, _, _ in inst], [v["x"] for _, v, _ in inst],
+                [v["r"] for _, v, _ in inst], [v["p"] for _, v, _ in inst],
+                [v["Ap"] for _, v, _ in inst], rdotr, [v["q"] for _, v, _ in inst],
+                [a for _, _, a in inst])
+    b.run()
+    torch.cuda.synchronize()
+    for (h, v, _), q in zip(inst, ref):
+        assert torch.equal(v["q"], q)

@@ -182,15 +182,16 @@ def test_large_block_boundaries(cuda, orc):
     assert h.info.maxRowSize == sizes.max()
 
 
-VARIANTS = [(0, 0, 0), (1, 0, 0), (1, 1, 1), (2, 0, 0), (2, 1, 0), (2, 1, 1), (3, 0, 1),
-            (3, 1, 0), (3, 1, 1), (4, 0, 0), (4, 1, 0), (4, 1, 1)]
+VARIANTS = [(0, 0, 0), (1, 0, 0), (1, 1, 1), (1, 2, 0), (2, 0, 0), (2, 1, 0), (2, 1, 1),
+            (2, 2, 0), (2, 2, 1), (3, 0, 1), (3, 1, 0), (3, 1, 1), (3, 2, 1), (4, 0, 0),
+            (4, 1, 0), (4, 1, 1), (4, 2, 1), (5, 0, 0), (5, 1, 1), (5, 2, 1)]
 KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.kernel.scatter", "ogs.order", "ogs.rows")
 
 
 def set_variant(kernel, order, rows):
     capi.tune_set("ogs.kernel", kernel)
     capi.tune_set("ogs.kernel.gather", kernel)
-    capi.tune_set("ogs.kernel.scatter", min(kernel, 3))
+    capi.tune_set("ogs.kernel.scatter", min(kernel, 4))
     capi.tune_set("ogs.order", order)
     capi.tune_set("ogs.rows", rows)
 
@@ -199,9 +200,10 @@ def set_variant(kernel, order, rows):
 @pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0)])
 def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, rows, box):
     """Block kernels, warp-chunk kernels (plain, pipelined, asynchronously staged
-    gathers, column-order scatter and gathers) in row and breadth-first chunk order,
-    with rows in CSR order or grouped by size: all give the reference's bits (each
-    row is still summed by one lane in CSR order)."""
+    gathers, column-order scatter and gathers, L2-prefetching gathers and scatter) in
+    row order, breadth-first chunk order and the renumbered breadth-first walk, with
+    rows in CSR order or grouped by size: all give the reference's bits (each row is
+    still summed by one lane in CSR order)."""
     nx, ny, nz, p, seed = box
     old = {k: capi.tune_get(k) for k in KNOBS}
     try:
@@ -230,7 +232,7 @@ def test_kernel_variants_and_chunk_orders(cuda, orc, kernel, order, rows, box):
             capi.tune_set(k, v)
 
 
-@pytest.mark.parametrize("kernel,rows", [(2, 1), (3, 0), (3, 1), (4, 0), (4, 1)])
+@pytest.mark.parametrize("kernel,rows", [(2, 1), (3, 0), (3, 1), (4, 0), (4, 1), (5, 1)])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
 @pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
 def test_variants_types_ops(cuda, orc, kernel, rows, dtype, op):
@@ -264,15 +266,17 @@ def test_variants_types_ops(cuda, orc, kernel, rows, dtype, op):
 
 
 @pytest.mark.parametrize("shift", [3, 6, 12])
-def test_page_sizes_of_breadth_first_order(cuda, orc, shift):
-    """Breadth-first chunk order over pages of 8, 64 and 4096 entries: the same bits."""
+@pytest.mark.parametrize("order", [1, 2])
+def test_page_sizes_of_breadth_first_order(cuda, orc, shift, order):
+    """Breadth-first chunk order, and the renumbered breadth-first walk, over pages
+    of 8, 64 and 4096 entries: the same bits."""
     old = {k: capi.tune_get(k) for k in KNOBS + ("ogs.page_shift",)}
     try:
-        set_variant(2, 1, 1)
+        set_variant(2, order, 1)
         capi.tune_set("ogs.page_shift", shift)
         ids = O.box_hex_ids(5, 4, 6, 3, 31)
         h, ref = make(orc, ids)
-        assert h.info.chunkOrder == 1 and h.info.NchunksT > 0
+        assert h.info.chunkOrder == order and h.info.NchunksT > 0
         rs, ci = ref["rsT"], ref["ciT"]
         q = orc.uniform(ids.size, 5)
         gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
