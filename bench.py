@@ -22,6 +22,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -106,11 +107,10 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_gpu{gpu}_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"sp_clocks_gpu{gpu}_{os.getpid()}.csv"
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",

@@ -171,7 +171,7 @@ sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, voi
                      sp_stream_t stream);
 
 /* ---------------------------------------------------------------- CG update
- * Full CG update (the spec form; the reference's BS5 only does the r update):
+ * Full CG update (x, r and r.r in one pass; the reference's BS5 only does the r update):
  *   x += alpha*p;  r -= alpha*Ap;  rdotr[0] = sum r*r   (FP64 result)
  * x = fma(alpha, p, x), r = fma(-alpha, Ap, r), accumulation fma(r, r, acc).
  * Scratch rules as for the fast reductions. */

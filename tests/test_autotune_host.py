@@ -1,0 +1,52 @@
+"""The autotuner's host logic (no GPU): plan configurations per degree, the kernel
+candidates of each, and the tuning table round trip."""
+import json
+
+from streamparanumal_gb300 import autotune
+
+
+def test_plan_configs_add_element_pages_and_renumbered_walk():
+    # p = 7: an element is 512 entries, the default page size
+    cfgs = autotune.plan_configs(7)
+    assert {(c["order"], c["rows"], c["page_shift"]) for c in cfgs} >= {
+        (1, 1, 9), (2, 1, 9), (1, 0, 9), (0, 1, 9), (0, 0, 9)}
+    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 1
+    # p = 3: 64-entry elements add pages of 2^6 for both breadth-first orders
+    cfgs = autotune.plan_configs(3)
+    assert {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": 6} in cfgs
+    assert {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": 6} in cfgs
+    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 2
+    # p = 1: 8-entry elements
+    assert min(c["page_shift"] for c in autotune.plan_configs(1)) == 3
+
+
+def test_kernel_candidates():
+    grouped = {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": 9}
+    plain_rows = {"order": 0, "rows": 0, "block_nnz": 2048, "page_shift": 9}
+    small_blocks = {"order": 0, "rows": 0, "block_nnz": 1024, "page_shift": 9}
+    assert autotune._kernels(grouped, "BS6") == [1, 2, 3, 4, 5]
+    assert autotune._kernels(grouped, "BS7") == [1, 2, 3, 4]
+    assert autotune._kernels(plain_rows, "BS8") == [0, 1, 2, 3, 4, 5]
+    assert autotune._kernels(plain_rows, "BS7") == [0, 1, 2]
+    assert autotune._kernels(small_blocks, "BS6") == [0]
+
+
+def test_table_round_trip(tmp_path):
+    table = {}
+    autotune.record(table, {"p": 5, "perm": True, "best": {"order": 2, "rows": 1,
+                                                              "page_shift": 8}})
+    autotune.record(table, {"p": 5, "perm": False, "best": {"order": 0, "rows": 1}})
+    path = tmp_path / "t.json"
+    autotune.save_table(table, path)
+    assert json.loads(path.read_text()) == table
+    assert autotune.load_table(path) == table
+    assert autotune.load_table(tmp_path / "missing.json") == {}
+
+
+def test_committed_table_is_well_formed():
+    table = autotune.load_table()
+    assert table, "the committed GB300 tuning table is missing"
+    for key, cfg in table.items():
+        assert key.startswith("p")
+        assert set(cfg) <= set(autotune.KNOBS)
+        assert cfg["order"] in (0, 1, 2) and cfg["kernel_gs"] in range(6)
