@@ -289,9 +289,12 @@ __device__ __forceinline__ RowRef global_row(const int32_t* __restrict__ rs, int
   return RowRef{__ldg(rs + d.x + r) - d.z, __ldg(rs + d.x + r + 1) - d.z, r};
 }
 
-// Row of the operator for walk row w (the walk is renumbered only under chunk order 2).
+// Row of the operator for walk row w: the walk is renumbered only under chunk order
+// 2 (PERM = 1); otherwise no lookup is compiled in.
+template <int PERM>
 __device__ __forceinline__ int32_t op_row(const int32_t* __restrict__ perm, int32_t w) {
-  return perm ? __ldg(perm + w) : w;
+  if constexpr (PERM != 0) return __ldg(perm + w);
+  return w;
 }
 
 template <typename T>
@@ -339,7 +342,7 @@ k_ogsw_gs_sym(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
     if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
 }
 
-template <typename T, int OP>
+template <typename T, int OP, int PERM = 0>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, const T* __restrict__ v, T* __restrict__ gv,
@@ -357,11 +360,11 @@ k_ogsw_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   __syncwarp();
   for (int32_t r = lane; r < nr; r += 32) {
     const RowRef q = staged_row(sm.rs[w], sm.ro[w], grouped, r);
-    gv[op_row(perm, ch.x + q.row)] = row_combine<T, OP>(sv, q.a, q.b);
+    gv[op_row<PERM>(perm, ch.x + q.row)] = row_combine<T, OP>(sv, q.a, q.b);
   }
 }
 
-template <typename T>
+template <typename T, int PERM = 0>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
                const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
@@ -381,7 +384,7 @@ k_ogsw_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
   }
   for (int32_t r = lane; r < nr; r += 32) {
     const RowRef q = global_row(rs, grouped, ch, r);
-    const T x = gv[op_row(perm, ch.x + q.row)];
+    const T x = gv[op_row<PERM>(perm, ch.x + q.row)];
     for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
   }
   __syncwarp();
@@ -412,7 +415,7 @@ __device__ __forceinline__ void prefetch_elem_l2(const void* p) {
 // PF = 1 (kernel 5): as soon as this chunk's values have landed, the next chunk's
 // values are prefetched into L2 from the column ids already in registers, so
 // they stream in while this chunk is combined and written back.
-template <typename T, int OP, int MODE, int PF = 0>  // MODE 0: gather+scatter (Sym), 1: gather
+template <typename T, int OP, int MODE, int PF = 0, int PERM = 0>  // MODE 0: gather+scatter, 1: gather
 __global__ void __launch_bounds__(kOgsThreads, kOgsPersistentCtas)
 k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped,
@@ -456,7 +459,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
       if (MODE == 0) {
         for (int32_t i = q.a; i < q.b; ++i) sv[i] = acc;
       } else {
-        gv[op_row(perm, d.x + q.row)] = acc;
+        gv[op_row<PERM>(perm, d.x + q.row)] = acc;
       }
     }
     __syncwarp();
@@ -475,7 +478,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   }
 }
 
-template <typename T>
+template <typename T, int PERM = 0>
 __global__ void __launch_bounds__(kOgsThreads, 4)
 k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
                const int32_t* __restrict__ ids, const T* __restrict__ gv, T* __restrict__ v,
@@ -498,7 +501,7 @@ k_ogsp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     load_cols(ids, dn, lane, coln);
     for (int32_t r = lane; r < nr; r += 32) {
       const RowRef q = global_row(rs, grouped, d, r);
-      const T x = gv[op_row(perm, d.x + q.row)];
+      const T x = gv[op_row<PERM>(perm, d.x + q.row)];
       for (int32_t i = q.a; i < q.b; ++i) sv[i] = x;
     }
     __syncwarp();
@@ -710,7 +713,7 @@ k_ogso_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 // the descriptor (one dependent round trip), there is no per-row loop, and the
 // stores of neighbouring lanes land on neighbouring addresses.  Copies only:
 // bit-identical to every other scatter.
-template <typename T>
+template <typename T, int PERM = 0>
 __global__ void __launch_bounds__(kOgsThreads, kOgsScatterCtas)
 k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ colS,
                const uint8_t* __restrict__ rowOf, const T* __restrict__ gv, T* __restrict__ v,
@@ -730,7 +733,7 @@ k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     col[u] = (i < sn) ? __ldg(colS + d.z + i) : 0;
     ro[u] = (i < sn) ? (int32_t)__ldg(rowOf + d.z + i) : 0;
   }
-  for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[op_row(perm, d.x + r)];
+  for (int32_t r = lane; r < nr; r += 32) sr[r] = gv[op_row<PERM>(perm, d.x + r)];
   __syncwarp();
 #pragma unroll
   for (int u = 0; u < kOgsPerLane; ++u)
@@ -843,11 +846,16 @@ static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
 template <typename T, int OP, int MODE>
 static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaStream_t s) {
   // a gather through a renumbered walk writes gv through perm: kernels 1, 2, 5 do
-  if (MODE == 1 && a.perm && (kv == 3 || kv == 4)) kv = 2;
+  const bool perm = MODE == 1 && a.perm;
+  if (perm && (kv == 3 || kv == 4)) kv = 2;
+  const unsigned pg = persistent_grid(a.nchunks, kOgsPersistentCtas);
   if (kv == 5) {
-    k_ogsp_gather<T, OP, MODE, 1><<<persistent_grid(a.nchunks, kOgsPersistentCtas), kOgsThreads,
-                                    0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped,
-                                            a.perm);
+    if (perm)
+      k_ogsp_gather<T, OP, MODE, 1, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
+                                                                 v, gv, a.grouped, a.perm);
+    else
+      k_ogsp_gather<T, OP, MODE, 1, 0><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
+                                                                 v, gv, a.grouped, nullptr);
   } else if (kv == 4 && a.e2s) {
     k_ogso_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.colS, a.e2s, v, gv, a.grouped);
@@ -855,15 +863,21 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
     k_ogsa_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
   } else if (kv >= 2) {
-    k_ogsp_gather<T, OP, MODE><<<persistent_grid(a.nchunks, kOgsPersistentCtas), kOgsThreads,
-                                 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped,
-                                         a.perm);
+    if (perm)
+      k_ogsp_gather<T, OP, MODE, 0, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
+                                                                 v, gv, a.grouped, a.perm);
+    else
+      k_ogsp_gather<T, OP, MODE, 0, 0><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
+                                                                 v, gv, a.grouped, nullptr);
   } else if (MODE == 0) {
     k_ogsw_gs_sym<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
                                                                      a.ids, v, a.grouped);
-  } else {
-    k_ogsw_gather<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
+  } else if (perm) {
+    k_ogsw_gather<T, OP, 1><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, a.perm);
+  } else {
+    k_ogsw_gather<T, OP, 0><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
+        a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr);
   }
 }
 
@@ -917,17 +931,27 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
         reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv,
         v, (int64_t)p->nnzT, (int64_t)p->NrowsT);
   } else if (kv >= 3 && !useN && p->d_colIdsST) {
-    k_ogss_scatter<T><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
-        reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv,
-        v, p->d_permT);
+    const int4* ch = reinterpret_cast<const int4*>(p->d_chunksT);
+    if (p->d_permT)
+      k_ogss_scatter<T, 1><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+          ch, p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv, v, p->d_permT);
+    else
+      k_ogss_scatter<T, 0><<<warp_grid(p->nchunksT), kOgsThreads, 0, s>>>(
+          ch, p->nchunksT, p->d_colIdsST, p->d_rowOfST, gv, v, nullptr);
   } else if (kv > 0) {
     const ChunkArgs a = useN ? chunks_n(p) : chunks_t(p);
-    if (kv >= 2)
-      k_ogsp_scatter<T><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+    if (kv >= 2 && a.perm)
+      k_ogsp_scatter<T, 1><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, a.perm);
+    else if (kv >= 2)
+      k_ogsp_scatter<T, 0><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, nullptr);
+    else if (a.perm)
+      k_ogsw_scatter<T, 1><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
           a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, a.perm);
     else
-      k_ogsw_scatter<T><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
-          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, a.perm);
+      k_ogsw_scatter<T, 0><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, gv, v, a.grouped, nullptr);
   } else if (useN) {
     if (p->NrowBlocksN == 0) return;
     k_ogs_scatter<T><<<dim3(p->NrowBlocksN, K), kOgsThreads, 0, s>>>(
