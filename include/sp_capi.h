@@ -74,8 +74,8 @@ void        sp_launch_count_reset(void);
  *    gather / scatter): 0 block kernels, 1 warp-chunk kernels, 2 pipelined
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
  *    the column-order scatter, 4 column-order pipelined gathers or the persistent
- *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch
- *    (gathers only); defaults 2, 2, 3.
+ *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch or
+ *    the column-major scatter (one thread per local column); defaults 2, 2, 5.
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);

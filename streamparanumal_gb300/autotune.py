@@ -43,7 +43,7 @@ def plan_configs(p: int) -> list[dict]:
 KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
            3: "warp-async-staged gathers / column-order scatter",
            4: "column-order gathers / persistent prefetching column-order scatter",
-           5: "pipelined gathers with L2 prefetch of the next chunk"}
+           5: "pipelined gathers with L2 prefetch of the next chunk / column-major scatter"}
 OPS = (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs"))
 
 
@@ -76,10 +76,12 @@ def _kernels(pc: dict, op: str) -> list[int]:
     """Kernel variants timed under one plan configuration: block kernels ignore the
     chunk order and row grouping, so they run once per block size; the column-order
     scatters ignore the row grouping, so they run under grouped plans only."""
-    ks = [0] if (pc["order"] == 0 and pc["rows"] == 0) else []
+    plain = pc["order"] == 0 and pc["rows"] == 0
+    ks = [0] if plain else []
     if pc["block_nnz"] == 2048:
         if op == "BS7":
-            ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else [])
+            # the column-major scatter (5) ignores chunks: timed once, with the plain plan
+            ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else []) + ([5] if plain else [])
         else:
             ks += [1, 2, 3, 4, 5]
     return ks
@@ -119,7 +121,10 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
     for order, rows, shift in sorted({t[:3] for t in timings}):
         choice, total = {"order": order, "rows": rows, "page_shift": shift}, 0.0
         for op, key in OPS:
-            cands = [t for t in timings if t[5] == op and (t[:3] == (order, rows, shift) or t[4] == 0)]
+            # block kernels and the column-major scatter do not depend on the chunk
+            # layout, so they compete under every plan configuration
+            cands = [t for t in timings if t[5] == op and (
+                t[:3] == (order, rows, shift) or t[4] == 0 or (op == "BS7" and t[4] == 5))]
             _, _, _, bnnz, k, _, ms = min(cands, key=lambda t: t[6])
             choice[key] = k
             if k == 0:

@@ -740,6 +740,21 @@ k_ogss_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* 
     if (lane + 32 * u < sn) v[col[u]] = sr[ro[u]];
 }
 
+// Column-major scatter (kernel 5 for scatters on T): one thread per local column,
+// v[i] = gv[row of i], so the stores of a warp are one contiguous run; the row
+// values are read where each column's row lies (rows numbered by first
+// appearance keep those reads mostly local).  Columns in no row are left alone.
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogsc_scatter(int32_t N, const int32_t* __restrict__ rowOfCol, const T* __restrict__ gv,
+               T* __restrict__ v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = __ldg(rowOfCol + i);
+    if (r >= 0) v[i] = gv[r];
+  }
+}
+
 // Persistent column-order scatter (kernel 4 for scatters on T chunks): as kernel 3,
 // with each warp walking chunks c, c+W, ... and bulk-prefetching the next chunk's
 // three contiguous ranges (column ids, row offsets, gv slice) into L2 before
@@ -925,6 +940,13 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
                            cudaStream_t s) {
   const bool useN = (trans == SP_TRANS);
   const int kv = variant(kTuneOgsKernelScatter, K, useN ? p->nchunksN : p->nchunksT);
+  if (kv == 5 && !useN && p->d_rowOfColT) {
+    const int64_t want = ((int64_t)p->N + kOgsThreads - 1) / kOgsThreads;
+    const int64_t cap = (int64_t)sm_count() * 64;
+    k_ogsc_scatter<T><<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), kOgsThreads, 0, s>>>(
+        p->N, p->d_rowOfColT, gv, v);
+    return;
+  }
   // the persistent prefetching scatter reads gv slices directly: not through perm
   if (kv == 4 && !useN && p->d_colIdsST && !p->d_permT) {
     k_ogssp_scatter<T><<<persistent_grid(p->nchunksT, kOgsScatterCtas), kOgsThreads, 0, s>>>(
@@ -1072,6 +1094,8 @@ static void free_plan_device(sp_ogs_plan* p) {
   if (p->d_walkCiT) cudaFree(p->d_walkCiT);
   if (p->d_permT) cudaFree(p->d_permT);
   p->d_walkRsT = p->d_walkCiT = p->d_permT = nullptr;
+  if (p->d_rowOfColT) cudaFree(p->d_rowOfColT);
+  p->d_rowOfColT = nullptr;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1270,6 +1294,12 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(colS, &p->d_colIdsST, s))) return st;
     if ((st = upload(rowOf, &p->d_rowOfST, s))) return st;
     if ((st = upload(e2s, &p->d_e2sT, s))) return st;
+    // the row of each local column, for the column-major scatter
+    std::vector<int32_t> rowOfCol(std::max(p->N, 1), -1);
+#pragma omp parallel for schedule(static)
+    for (int32_t r = 0; r < p->NrowsT; ++r)
+      for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) rowOfCol[p->colIdsT[i]] = r;
+    if ((st = upload(rowOfCol, &p->d_rowOfColT, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   } else {
     p->nchunksT = p->nchunksN = 0;

@@ -124,6 +124,9 @@ struct sp_ogs_plan {
   int32_t* d_colIdsST = nullptr;     // nnzT
   uint8_t* d_rowOfST = nullptr;      // nnzT
   uint8_t* d_e2sT = nullptr;         // nnzT: sorted position of each row-order entry
+  // the row of T holding each local column (-1: in no row), for the column-major
+  // scatter; built with the warp chunks
+  int32_t* d_rowOfColT = nullptr;    // N
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
   bool own_blocks_n = false;      // d_blocksN is a separate allocation
 

@@ -37,7 +37,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.order", 0, 2, {1}},
     {"reduce.rolling", 0, 1, {1}},
     {"ogs.kernel.gather", 0, 5, {2}},
-    {"ogs.kernel.scatter", 0, 4, {3}},
+    {"ogs.kernel.scatter", 0, 5, {5}},
     {"ogs.rows", 0, 1, {1}},
     {"ogs.page_shift", 3, 16, {9}},
 };

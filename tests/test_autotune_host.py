@@ -27,7 +27,7 @@ def test_kernel_candidates():
     assert autotune._kernels(grouped, "BS6") == [1, 2, 3, 4, 5]
     assert autotune._kernels(grouped, "BS7") == [1, 2, 3, 4]
     assert autotune._kernels(plain_rows, "BS8") == [0, 1, 2, 3, 4, 5]
-    assert autotune._kernels(plain_rows, "BS7") == [0, 1, 2]
+    assert autotune._kernels(plain_rows, "BS7") == [0, 1, 2, 5]
     assert autotune._kernels(small_blocks, "BS6") == [0]
 
 

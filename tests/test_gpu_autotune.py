@@ -19,9 +19,9 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
                              "kernel_scatter", "block_nnz"}
         # grouped plans (2, plus 64-entry pages at p = 3, plus the renumbered walk) x
         # (5 + 4 + 5) kernels, the breadth-first CSR plan x (5 + 2 + 5), the row-order
-        # CSR plan with block kernels too (6 + 3 + 6), and block kernels at
-        # block_nnz 1024 (3)
-        assert len(res["candidates"]) == 56 + 12 + 15 + 3
+        # CSR plan with block kernels and the column-major scatter too (6 + 4 + 6), and
+        # block kernels at block_nnz 1024 (3)
+        assert len(res["candidates"]) == 56 + 12 + 16 + 3
         table = {}
         autotune.record(table, res)
         path = tmp_path / "t.json"

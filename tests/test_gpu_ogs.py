@@ -191,7 +191,7 @@ KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.kernel.scatter", "ogs.order", "
 def set_variant(kernel, order, rows):
     capi.tune_set("ogs.kernel", kernel)
     capi.tune_set("ogs.kernel.gather", kernel)
-    capi.tune_set("ogs.kernel.scatter", min(kernel, 4))
+    capi.tune_set("ogs.kernel.scatter", kernel)
     capi.tune_set("ogs.order", order)
     capi.tune_set("ogs.rows", rows)
 
