@@ -146,8 +146,20 @@ def load_table(path: Path = TABLE) -> dict:
 
 
 def save_table(table: dict, path: Path = TABLE) -> None:
+    """Writes the table as JSON and, beside it, the text form the BS6-BS8 drivers
+    read (one line per key: `p7_perm ogs.order=1 ogs.rows=1 ...`)."""
     path.parent.mkdir(parents=True, exist_ok=True)
     path.write_text(json.dumps(table, indent=1, sort_keys=True) + "\n")
+    path.with_suffix(".txt").write_text(table_text(table))
+
+
+def table_text(table: dict) -> str:
+    lines = []
+    for key in sorted(table):
+        cfg = table[key]
+        lines.append(" ".join([key] + [f"{KNOBS[k]}={int(cfg[k])}" for k in sorted(cfg)
+                                       if k in KNOBS]))
+    return "\n".join(lines) + "\n"
 
 
 def record(table: dict, result: dict) -> None:

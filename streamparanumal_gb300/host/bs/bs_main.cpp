@@ -41,6 +41,7 @@ int main(int argc, char** argv) {
     } else if (which <= 5) {
       bsVecRun(which, platform, settings);
     } else {
+      bsOgsApplyTuning(settings);
       mesh_t mesh(platform, settings, comm);
       bsOgsRun(which, platform, settings, mesh);
     }

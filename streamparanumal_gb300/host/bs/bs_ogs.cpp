@@ -4,6 +4,13 @@
 // operators on FP32 node data (byte accounting with 4-byte values).
 #include "bs.hpp"
 
+#include <unistd.h>
+
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
+
 namespace libp {
 
 void bsOgsSettings(settings_t& s) {
@@ -11,6 +18,56 @@ void bsOgsSettings(settings_t& s) {
   meshAddSettings(s);
   s.newSetting("-fp", "--precision", "PRECISION", "FP64", "Storage precision", {"FP64", "FP32"});
   s.newSetting("-v", "--verbose", "VERBOSE", "FALSE", "Enable verbose output", {"TRUE", "FALSE"});
+  s.newSetting("-t", "--tuning", "TUNING FILE", "DEFAULT",
+               "Per-degree kernel table (DEFAULT: the package's, NONE: library defaults)");
+}
+
+// The table's text form holds one line per degree and layout:
+//   p7_perm ogs.order=1 ogs.rows=1 ogs.kernel=2 ...
+// The line for this run's degree (and permuted layout, else the plain one) is
+// applied through sp_tune_set.
+void bsOgsApplyTuning(settings_t& s) {
+  std::string file;
+  s.getSetting("TUNING FILE", file);
+  if (file == "NONE") return;
+  if (file == "DEFAULT") {
+    char exe[4096];
+    const ssize_t len = readlink("/proc/self/exe", exe, sizeof(exe) - 1);
+    if (len <= 0) return;
+    exe[len] = 0;
+    std::string dir(exe);
+    dir = dir.substr(0, dir.find_last_of('/'));          // .../bin
+    file = dir.substr(0, dir.find_last_of('/')) + "/tuning/gb300.txt";
+  }
+  std::ifstream in(file);
+  if (!in) {
+    LIBP_ABORT("Cannot read tuning file " << file, !s.compareSetting("TUNING FILE", "DEFAULT"));
+    return;
+  }
+  int p = 0;
+  long long seed = 0;
+  s.getSetting("POLYNOMIAL DEGREE", p);
+  if (s.hasSetting("PERMUTATION SEED")) s.getSetting("PERMUTATION SEED", seed);
+  const std::string want = "p" + std::to_string(p), wantPerm = want + "_perm";
+  std::string line, plain, perm;
+  while (std::getline(in, line)) {
+    const std::string key = line.substr(0, line.find(' '));
+    if (key == want) plain = line;
+    if (key == wantPerm) perm = line;
+  }
+  const std::string& use = (seed != 0 && !perm.empty()) ? perm : plain;
+  std::istringstream fields(use);
+  std::string field;
+  fields >> field;  // the key
+  while (fields >> field) {
+    const size_t eq = field.find('=');
+    if (eq == std::string::npos) continue;
+    const std::string knob = field.substr(0, eq);
+    const long long value = std::stoll(field.substr(eq + 1));
+    checkStatus(sp_tune_set(knob.c_str(), value), "tuning file");
+  }
+  if (s.compareSetting("VERBOSE", "TRUE") && !use.empty())
+    std::printf("tuning: %s\n", use.c_str());
 }
 
 namespace {

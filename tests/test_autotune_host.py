@@ -50,3 +50,13 @@ def test_committed_table_is_well_formed():
         assert key.startswith("p")
         assert set(cfg) <= set(autotune.KNOBS)
         assert cfg["order"] in (0, 1, 2) and cfg["kernel_gs"] in range(6)
+
+
+def test_text_form_matches_the_table():
+    """The drivers read the text form; it carries the same knobs as the JSON."""
+    table = autotune.load_table()
+    txt = autotune.TABLE.with_suffix(".txt").read_text()
+    assert txt == autotune.table_text(table)
+    line = next(ln for ln in txt.splitlines() if ln.split()[0] == "p7_perm")
+    fields = dict(f.split("=") for f in line.split()[1:])
+    assert {autotune.KNOBS[k]: str(v) for k, v in table["p7_perm"].items()} == fields

@@ -84,3 +84,21 @@ def test_bs6_to_bs8_rows(cuda, bsdir, which, title, extra):
     assert m, out
     assert int(m.group(1)) == 3
     assert int(m.group(2)) == (6 * 3 + 1) * (5 * 3 + 1) * (4 * 3 + 1)
+
+
+@pytest.mark.gpu
+def test_bs8_applies_the_tuning_table(cuda, bsdir, tmp_path):
+    out = run(bsdir, "BS8", "-nx", 3, "-ny", 3, "-nz", 3, "-p", 3, "-v", "TRUE").stdout
+    assert "tuning: p3 " in out
+    out = run(bsdir, "BS8", "-nx", 3, "-ny", 3, "-nz", 3, "-p", 3, "-ps", 5, "-v", "TRUE").stdout
+    assert "tuning: p3_perm " in out
+    out = run(bsdir, "BS8", "-nx", 3, "-ny", 3, "-nz", 3, "-p", 3, "-t", "NONE", "-v",
+              "TRUE").stdout
+    assert "tuning:" not in out
+    table = tmp_path / "t.txt"
+    table.write_text("p3 ogs.order=0 ogs.rows=0 ogs.kernel=0\n")
+    out = run(bsdir, "BS8", "-nx", 3, "-ny", 3, "-nz", 3, "-p", 3, "-t", table, "-v",
+              "TRUE").stdout
+    assert "tuning: p3 ogs.order=0 ogs.rows=0 ogs.kernel=0" in out
+    res = run(bsdir, "BS8", "-p", 3, "-t", tmp_path / "missing.txt", check=False)
+    assert res.returncode == 1 and "Cannot read tuning file" in res.stderr
