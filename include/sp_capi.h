@@ -258,6 +258,94 @@ sp_status sp_ogs_scatter(const sp_ogs_plan* plan, sp_type type, sp_transpose tra
 sp_status sp_ogs_gather_scatter(const sp_ogs_plan* plan, sp_type type, sp_op op,
                                 sp_transpose trans, int32_t k, void* v, sp_stream_t stream);
 
+/* ---------------------------------------------------------------- multi-rank ogs
+ * ogs_t::Setup over a communicator of several ranks (libs/ogs/ogsSetup.cpp:87-290:
+ * FindSharedGroups :292-469, ConstructSharedNodes :617-813) with the Pairwise
+ * exchange (libs/ogs/ogsPairwise.cpp:176-387).  Each rank holds its own local
+ * nodes.  Groups whose members all sit on this rank form the local operator, groups
+ * shared with other ranks the halo operator; a pairwise exchange of gathered halo
+ * rows joins the halo groups across ranks.  The library has no transport of its
+ * own: setup talks through the caller's sp_comm callbacks, and the data exchange is
+ * made by the caller between sp_ogs_mr_exchange_start and sp_ogs_mr_exchange_finish,
+ * following sp_ogs_mr_schedule (one message per peer and direction, as the
+ * Isend/Irecv pairs of ogsPairwise_t::DeviceFinish, ogsPairwise.cpp:125-156).
+ *
+ * Callbacks return 0 on success (anything else fails the setup with SP_ERR_COMM).
+ *   alltoallv: this rank sends sendcounts[r] elements of elem_bytes bytes, from
+ *     element sdispls[r] of `send`, to rank r and receives recvcounts[r] elements
+ *     from rank r at element rdispls[r] of `recv` (MPI_Alltoallv);
+ *   allreduce_i64: *value <- op over all ranks (op 0 sum, 1 min, 2 max). */
+#define SP_ERR_COMM           9  /* an sp_comm callback reported a failure          */
+typedef struct {
+  int32_t rank;
+  int32_t size;
+  void* ctx;
+  int32_t (*alltoallv)(void* ctx, const void* send, const int64_t* sendcounts,
+                       const int64_t* sdispls, void* recv, const int64_t* recvcounts,
+                       const int64_t* rdispls, int32_t elem_bytes);
+  int32_t (*allreduce_i64)(void* ctx, int64_t* value, int32_t op);
+} sp_comm;
+
+typedef struct sp_ogs_mr sp_ogs_mr;
+
+typedef struct {
+  int32_t N;
+  int32_t NlocalP, NlocalT;  /* local operator rows: with a positive member / all     */
+  int32_t NhaloP, NhaloT;    /* halo operator rows: with a positive member here / all */
+  int32_t Nshared;           /* (halo row, remote rank) pairs                         */
+  int32_t gather_defined;    /* every group has exactly one positive member           */
+  int32_t uploaded;          /* device operators exist                                */
+  int64_t Ngather;           /* NlocalP + NhaloP                                      */
+  int64_t NgatherGlobal;     /* Ngather summed over the ranks                         */
+} sp_ogs_mr_info;
+
+/* Exchange schedule of one transpose mode (ogsPairwise_t::data_t).  Send side: the
+ * Nsend halo rows sendIds[] are packed into the send buffer, peer i of the send
+ * list gets sendCounts[i]*k values from element sendOffsets[i]*k.  Receive side:
+ * the halo buffer holds this rank's NrowsP rows first; peer j of the receive list
+ * delivers recvCounts[j]*k values at element (NrowsP + recvOffsets[j])*k.  The
+ * post-exchange gather reduces the Ncols = NrowsP + received columns into Nrows
+ * rows (CSR postRowStarts/postColIds: this rank's row first, then the other ranks'
+ * values in ascending rank order). */
+typedef struct {
+  int32_t Nsend, NrowsP, Nrows, Ncols;
+  int32_t NranksSend, NranksRecv;
+} sp_ogs_mr_sched;
+
+/* Collective over comm.  h_ids[N] as sp_ogs_setup (signs written back with
+ * unique).  upload == 0 builds the host half only (operators and schedules, no
+ * device use); otherwise the operators are uploaded on `stream`. */
+sp_status sp_ogs_mr_setup(int32_t N, int64_t* h_ids, sp_kind kind, int32_t unique,
+                          const sp_comm* comm, int32_t upload, sp_stream_t stream,
+                          sp_ogs_mr** out);
+sp_status sp_ogs_mr_destroy(sp_ogs_mr* h);
+sp_status sp_ogs_mr_info_get(const sp_ogs_mr* h, sp_ogs_mr_info* info);
+/* Device operators (NULL before upload): which 0 = local, 1 = halo. */
+const sp_ogs_plan* sp_ogs_mr_plan(const sp_ogs_mr* h, int32_t which);
+/* Host CSR of the local (which 0) or halo (1) operator: op SP_TRANS -> T,
+ * SP_NOTRANS -> N.  Arrays sized rows+1 and entries (either may be NULL). */
+sp_status sp_ogs_mr_csr(const sp_ogs_mr* h, int32_t which, sp_transpose op,
+                        int32_t* h_rowStarts, int32_t* h_colIds);
+/* Schedule of one mode; any array may be NULL (sizes NranksSend, NranksRecv,
+ * Nsend, Nrows + 1, Ncols). */
+sp_status sp_ogs_mr_schedule(const sp_ogs_mr* h, sp_transpose mode, sp_ogs_mr_sched* s,
+                             int32_t* h_sendRanks, int32_t* h_sendCounts,
+                             int32_t* h_sendOffsets, int32_t* h_recvRanks,
+                             int32_t* h_recvCounts, int32_t* h_recvOffsets,
+                             int32_t* h_sendIds, int32_t* h_postRowStarts,
+                             int32_t* h_postColIds);
+/* Device halves of one exchange (ogsPairwise_t::DeviceStart / DeviceFinish without
+ * the transport, ogsPairwise.cpp:106-156):
+ *   start:  send[n*k + f] = halo[sendIds[n]*k + f]    (extract, ogsKernels.okl:167-177)
+ *   finish: out[row*k + f] = op over the columns c of row, in CSR order, of
+ *           halo[c*k + f]                              (the post-exchange gather)
+ * halo holds Ncols*k values of the mode, send Nsend*k, out Nrows*k. */
+sp_status sp_ogs_mr_exchange_start(const sp_ogs_mr* h, sp_type type, sp_transpose mode,
+                                   int32_t k, const void* halo, void* send, sp_stream_t stream);
+sp_status sp_ogs_mr_exchange_finish(const sp_ogs_mr* h, sp_type type, sp_op op,
+                                    sp_transpose mode, int32_t k, const void* halo, void* out,
+                                    sp_stream_t stream);
+
 /* ---------------------------------------------------------------- batched instances
  * Many independent instances of uneven size in ONE persistent launch.  Instance i
  * owns x[i], r[i], p[i], Ap[i] (n[i] doubles), rdotr[i] (one double) and alpha[i],
@@ -297,6 +385,14 @@ sp_status sp_mesh_box_hex_ids(int32_t nx, int32_t ny, int32_t nz, int32_t p, uin
  * synchronises `stream`. */
 sp_status sp_mesh_box_hex_ids_device(int32_t nx, int32_t ny, int32_t nz, int32_t p,
                                      uint64_t perm_seed, int64_t* d_ids, sp_stream_t stream);
+/* Ids of rank `rank` when `size` ranks each hold an nx*ny*nz box (mesh_t::SetupBoxHex3D
+ * with the Factor3 / RankDecomp3 rank grid, libs/mesh/meshSetupBoxHex3D.cpp:44-53,
+ * libs/core/rankDecomp.cpp; ConnectNodes across ranks numbers local node l of rank
+ * r as r*E*Np + l): id = 1 + the smallest such global index on the same global
+ * lattice point.  size == 1 gives sp_mesh_box_hex_ids. */
+sp_status sp_mesh_box_hex_ids_rank(int32_t nx, int32_t ny, int32_t nz, int32_t p,
+                                   uint64_t perm_seed, int32_t size, int32_t rank,
+                                   int64_t* h_ids);
 
 #ifdef __cplusplus
 }

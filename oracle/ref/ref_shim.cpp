@@ -9,10 +9,48 @@
 //   * matrixInverse / matrixRightSolve: Gauss-Jordan elimination with partial pivoting.
 // Only node coordinates depend on these, and coordinates only enter tolerance-based
 // face matching; the global ids of a box mesh do not depend on their last bits.
+// Also the shared state of the MPI stand-in (shim/mpi.h).
+#include <sys/mman.h>
+
 #include <cmath>
 #include <vector>
 
 #include "platform.hpp"
+
+struct sp_mpi_world* sp_mpi_w = nullptr;
+int sp_mpi_rank = 0;
+size_t sp_mpi_type_size[4096] = {0, 1, 4, 8, 4, 8};
+int sp_mpi_ntypes = 6;
+struct sp_mpi_req sp_mpi_reqs[SP_MPI_MAXREQ];
+int sp_mpi_ncomms = MPI_COMM_WORLD;
+
+int sp_mpi_start(int size, size_t area_bytes, size_t box_bytes) {
+  if (size < 1 || size > SP_MPI_MAXRANKS) return 1;
+  const size_t total = sizeof(sp_mpi_world) + (size_t)size * (area_bytes + box_bytes);
+  void* p = mmap(nullptr, total, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED) return 1;
+  sp_mpi_world* w = static_cast<sp_mpi_world*>(p);
+  w->size = size;
+  w->area_bytes = area_bytes;
+  w->box_bytes = box_bytes;
+  pthread_barrierattr_t ba;
+  pthread_barrierattr_init(&ba);
+  pthread_barrierattr_setpshared(&ba, PTHREAD_PROCESS_SHARED);
+  pthread_barrier_init(&w->bar, &ba, (unsigned)size);
+  pthread_mutexattr_t ma;
+  pthread_mutexattr_init(&ma);
+  pthread_mutexattr_setpshared(&ma, PTHREAD_PROCESS_SHARED);
+  pthread_mutex_init(&w->mtx, &ma);
+  pthread_condattr_t ca;
+  pthread_condattr_init(&ca);
+  pthread_condattr_setpshared(&ca, PTHREAD_PROCESS_SHARED);
+  pthread_cond_init(&w->cv, &ca);
+  for (int r = 0; r < size; ++r) w->box[r].nmsg = w->box[r].live = 0, w->box[r].used = 0;
+  sp_mpi_w = w;
+  return 0;
+}
+
+void sp_mpi_set_rank(int rank) { sp_mpi_rank = rank; }
 
 namespace libp {
 

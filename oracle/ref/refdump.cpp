@@ -9,9 +9,19 @@
 //       the host overloads of GatherScatter(Add, Sym), Gather(Add, Trans),
 //       Gather(Add, NoTrans) and Scatter(NoTrans); also the row of every local
 //       index (Scatter of the row numbers) and the ids after Setup.
+//   refdump ogsmr <size> <nx> <ny> <nz> <p> <qseed> <outdir>
+//       the same on `size` ranks (forked processes meeting through the MPI
+//       stand-in), each holding an nx*ny*nz box: per rank r, files r<r>_*.bin with
+//       the box ids (mesh_t, unsigned), the ids after the mesh's ogs Setup (signed),
+//       the counts of a Pairwise handle built on those signed ids, and its
+//       GatherScatter (Sym / NoTrans / Trans, Add; Sym, Max), Gather (Trans /
+//       NoTrans / Sym, Add) and Scatter (NoTrans / Trans / Sym) on seeded values.
 //   refdump bs <N> <seed> <outdir>
 //       the BS1-BS5 OKL kernels translated for OCCA Serial execution (okl2cpp.py)
 //       on seeded inputs.
+#include <sys/wait.h>
+#include <unistd.h>
+
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -129,6 +139,90 @@ int run_ogs(int argc, char** argv) {
   return 0;
 }
 
+int ogsmr_rank(const std::string& nx, const std::string& ny, const std::string& nz,
+               const std::string& p, uint64_t qseed, const std::string& out) {
+  std::vector<std::string> args = {"refdump", "-m", "Serial", "-e", "Hex", "-nx", nx,
+                                   "-ny", ny, "-nz", nz, "-p", p};
+  std::vector<char*> av;
+  for (auto& s : args) av.push_back(const_cast<char*>(s.c_str()));
+  comm_t comm(Comm::World().Dup());
+  const int rank = comm.rank();
+  refSettings_t settings((int)av.size(), av.data(), comm);
+  platform_t platform(settings);
+  mesh_t mesh(platform, settings, comm);
+  const dlong N = mesh.Nelements * mesh.Np;
+  const std::string pre = out + "/r" + std::to_string(rank) + "_";
+  auto put = [&](const std::string& name, auto* ptr, size_t n) { dump(out, "r" + std::to_string(rank) + "_" + name, ptr, n); };
+  (void)pre;
+
+  // the mesh's own handle (Auto, unique) flagged one owner per group
+  memory<hlong> ids = mesh.globalIds.clone();
+  memory<hlong> absIds(N);
+  for (dlong l = 0; l < N; ++l) absIds[l] = std::abs(ids[l]);
+  put("box_ids", absIds.ptr(), N);
+  put("ids", ids.ptr(), N);
+
+  ogs::ogs_t pw;
+  pw.Setup(N, ids, comm, ogs::Signed, ogs::Pairwise, false, false, platform);
+  const long long counts[8] = {pw.N, pw.NlocalP, pw.NlocalT, pw.NhaloP, pw.NhaloT, pw.Ngather,
+                               (long long)pw.NgatherGlobal, pw.gather_defined ? 1 : 0};
+  put("counts", counts, 8);
+
+  const dlong G = pw.NlocalT + pw.NhaloT;
+  memory<double> q(N), g(G > 0 ? G : 1);
+  uniform(N, qseed + 1000 * rank, q.ptr());
+  uniform(G, qseed + 1000 * rank + 1, g.ptr());
+  put("q", q.ptr(), N);
+  put("g", g.ptr(), G);
+  const ogs::Transpose modes[3] = {ogs::Sym, ogs::NoTrans, ogs::Trans};
+  const char* names[3] = {"sym", "notrans", "trans"};
+  for (int m = 0; m < 3; ++m) {
+    memory<double> v = q.clone();
+    pw.GatherScatter(v, 1, ogs::Add, modes[m]);
+    put(std::string("gs_") + names[m], v.ptr(), N);
+    memory<double> gv(G > 0 ? G : 1);
+    for (dlong i = 0; i < G; ++i) gv[i] = 0.0;
+    pw.Gather(gv, q, 1, ogs::Add, modes[m]);
+    put(std::string("gather_") + names[m], gv.ptr(), G);
+    memory<double> vs(N);
+    for (dlong i = 0; i < N; ++i) vs[i] = 0.0;
+    pw.Scatter(vs, g, 1, modes[m]);
+    put(std::string("scatter_") + names[m], vs.ptr(), N);
+  }
+  memory<double> vm = q.clone();
+  pw.GatherScatter(vm, 1, ogs::Max, ogs::Sym);
+  put("gs_sym_max", vm.ptr(), N);
+  return 0;
+}
+
+int run_ogsmr(int argc, char** argv) {
+  if (argc < 9) return 2;
+  const int size = std::atoi(argv[2]);
+  const std::string nx = argv[3], ny = argv[4], nz = argv[5], p = argv[6];
+  const uint64_t qseed = std::strtoull(argv[7], nullptr, 10);
+  const std::string out = argv[8];
+  if (sp_mpi_start(size, (size_t)256 << 20, (size_t)64 << 20)) return 1;
+  std::vector<pid_t> kids;
+  for (int r = 0; r < size; ++r) {
+    const pid_t pid = fork();
+    if (pid < 0) return 1;
+    if (pid == 0) {
+      sp_mpi_set_rank(r);
+      std::fflush(stdout);
+      _exit(ogsmr_rank(nx, ny, nz, p, qseed, out));
+    }
+    kids.push_back(pid);
+  }
+  int rc = 0;
+  for (pid_t k : kids) {
+    int st = 0;
+    waitpid(k, &st, 0);
+    if (!WIFEXITED(st) || WEXITSTATUS(st) != 0) rc = 1;
+  }
+  std::printf("ogsmr size=%d rc=%d\n", size, rc);
+  return rc;
+}
+
 }  // namespace
 
 // BS1-BS5 kernels (OCCA Serial translation of the reference's OKL)
@@ -187,6 +281,7 @@ int main(int argc, char** argv) {
   Comm::Init(argc, argv);
   int rc = 2;
   if (argc > 1 && std::string(argv[1]) == "ogs") rc = run_ogs(argc, argv);
+  else if (argc > 1 && std::string(argv[1]) == "ogsmr") rc = run_ogsmr(argc, argv);
   else if (argc > 1 && std::string(argv[1]) == "bs") rc = run_bs(argc, argv);
   if (rc == 2) std::fprintf(stderr, "usage: refdump ogs nx ny nz p perm_seed qseed outdir | bs N seed outdir\n");
   Comm::Finalize();

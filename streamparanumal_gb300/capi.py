@@ -25,6 +25,7 @@ SP_ERR_SIZE = 5
 SP_ERR_CSR = 6
 SP_ERR_TIMEOUT = 7
 SP_ERR_DEVICE_CHECK = 8
+SP_ERR_COMM = 9
 
 # enums shared with the reference's ogs::Type / Op / Transpose / Kind
 FLOAT, DOUBLE, INT32, INT64 = 0, 1, 2, 3
@@ -47,6 +48,17 @@ class OgsInfo(ctypes.Structure):
                 ("nnzN", c_int32), ("NrowBlocksT", c_int32), ("NrowBlocksN", c_int32),
                 ("maxRowSize", c_int32), ("NgatherGlobal", c_int64), ("NchunksT", c_int32),
                 ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32)]
+
+
+class MrInfo(ctypes.Structure):
+    _fields_ = [("N", c_int32), ("NlocalP", c_int32), ("NlocalT", c_int32), ("NhaloP", c_int32),
+                ("NhaloT", c_int32), ("Nshared", c_int32), ("gather_defined", c_int32),
+                ("uploaded", c_int32), ("Ngather", c_int64), ("NgatherGlobal", c_int64)]
+
+
+class MrSched(ctypes.Structure):
+    _fields_ = [("Nsend", c_int32), ("NrowsP", c_int32), ("Nrows", c_int32), ("Ncols", c_int32),
+                ("NranksSend", c_int32), ("NranksRecv", c_int32)]
 
 
 _P = c_void_p
@@ -106,10 +118,23 @@ SIGNATURES = {
     "sp_mesh_box_hex_ids": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _I64P]),
     "sp_mesh_box_hex_ids_device": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, _P,
                                              _P]),
+    "sp_mesh_box_hex_ids_rank": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_uint64, c_int32,
+                                           c_int32, _I64P]),
+    "sp_ogs_mr_setup": (c_int32, [c_int32, _I64P, c_int32, c_int32, _P, c_int32, _P,
+                                  POINTER(c_void_p)]),
+    "sp_ogs_mr_destroy": (c_int32, [_P]),
+    "sp_ogs_mr_info_get": (c_int32, [_P, POINTER(MrInfo)]),
+    "sp_ogs_mr_plan": (c_void_p, [_P, c_int32]),
+    "sp_ogs_mr_csr": (c_int32, [_P, c_int32, c_int32, _I32P, _I32P]),
+    "sp_ogs_mr_schedule": (c_int32, [_P, c_int32, POINTER(MrSched), _I32P, _I32P, _I32P, _I32P,
+                                     _I32P, _I32P, _I32P, _I32P, _I32P]),
+    "sp_ogs_mr_exchange_start": (c_int32, [_P, c_int32, c_int32, c_int32, _P, _P, _P]),
+    "sp_ogs_mr_exchange_finish": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P, _P]),
 }
 
 _STATUS_FREE = {"sp_last_error_string", "sp_status_string", "sp_version", "sp_launch_count",
-                "sp_launch_count_reset", "sp_reduce_scratch_bytes", "sp_ogs_block_nnz"}
+                "sp_launch_count_reset", "sp_reduce_scratch_bytes", "sp_ogs_block_nnz",
+                "sp_ogs_mr_plan"}
 
 _lib: ctypes.CDLL | None = None
 

@@ -1263,9 +1263,11 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       }
       return q;
     };
-    const bool same = !renumber && (chunksN == chunksT);
+    // N shares T's descriptors only when row AND entry ranges agree (equal row
+    // ranges alone are not enough: N rows keep only the positive members)
     chunksT = quads(chunksT, wrs);
-    chunksN = same ? chunksT : quads(chunksN, p->rowStartsN.data());
+    chunksN = quads(chunksN, p->rowStartsN.data());
+    const bool same = !renumber && (chunksN == chunksT);
     if ((st = upload(chunksT, &p->d_chunksT, s))) return st;
     if (same) {
       p->d_chunksN = p->d_chunksT;

@@ -83,6 +83,22 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
 // stored (identity for perm_seed 0, else a seeded Fisher-Yates shuffle).
 std::vector<int32_t> box_slots(int64_t E, uint64_t perm_seed);
 
+// Knuth MMIX linear congruential generator with the reference's constants and
+// seeding (random.cpp:47-100): x_{n+1} = a*x_n + c (mod 2^64), state_0 = a*(~0 ^ seed) + c,
+// draw = |(int)x| (low 32 bits as a signed int).
+struct Lcg {
+  static constexpr uint64_t A = 6364136223846793005ULL;
+  static constexpr uint64_t C = 1ULL;
+  uint64_t x;
+  explicit Lcg(uint64_t seed) : x(A * (~0ULL ^ seed) + C) {}
+  int32_t next_int() {
+    const int32_t v = (int32_t)(uint32_t)x;
+    x = A * x + C;
+    // abs of INT_MIN stays INT_MIN in two's complement, as std::abs does in practice
+    return (v < 0) ? (int32_t)(0u - (uint32_t)v) : v;
+  }
+};
+
 }  // namespace sp
 
 struct sp_ogs_plan {

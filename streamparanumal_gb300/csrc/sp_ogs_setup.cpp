@@ -24,22 +24,6 @@
 
 namespace sp {
 
-// Knuth MMIX linear congruential generator with the reference's constants and
-// seeding (random.cpp:47-100): x_{n+1} = a*x_n + c (mod 2^64), state_0 = a*(~0 ^ seed) + c,
-// draw = |(int)x| (low 32 bits as a signed int).
-struct Lcg {
-  static constexpr uint64_t A = 6364136223846793005ULL;
-  static constexpr uint64_t C = 1ULL;
-  uint64_t x;
-  explicit Lcg(uint64_t seed) : x(A * (~0ULL ^ seed) + C) {}
-  int32_t next_int() {
-    const int32_t v = (int32_t)(uint32_t)x;
-    x = A * x + C;
-    // abs of INT_MIN stays INT_MIN in two's complement, as std::abs does in practice
-    return (v < 0) ? (int32_t)(0u - (uint32_t)v) : v;
-  }
-};
-
 static inline int64_t iabs64(int64_t v) { return v < 0 ? -v : v; }
 
 // Groups of |id| as (key, member list ascending local index), keys ascending.

@@ -6,7 +6,9 @@ plus its BS1-BS5 OKL kernels lowered for OCCA Serial execution -- and records
 SHA-256 digests and a few leading values of every output, together with the
 inputs' seeds, in tests/golden/*.json.  Small cases also keep the reference's
 signed ids (after its unique-owner flagging) so the N-operator paths can be
-checked against the reference's own owners.
+checked against the reference's own owners.  The multi-rank cases run the
+reference on several forked ranks that meet through the MPI stand-in of
+oracle/ref/shim/mpi.h.
 
 Needs the reference tree (build with `make -C oracle/ref`); the committed fixtures
 are what the tests read.  Usage: python tests/golden/make_golden.py
@@ -38,6 +40,18 @@ OGS_CASES = [
     (16, 16, 16, 7, 0, 2024),   # BS8 anchor configuration: 2,097,152 local nodes
 ]
 KEEP_IDS_MAX = 40000
+# multi-rank: (ranks, nx, ny, nz, p, qseed), nx*ny*nz elements per rank.  Rank counts
+# are powers of two: the reference's mesh setup also builds its CrystalRouter
+# exchange (Auto method), whose setup leaves messages unmatched at other counts.
+OGSMR_CASES = [
+    (2, 2, 2, 2, 2, 31),
+    (4, 2, 3, 2, 3, 32),
+    (8, 2, 2, 2, 2, 33),
+    (2, 3, 3, 3, 5, 34),
+]
+OGSMR_OUTPUTS = ["gs_sym", "gs_notrans", "gs_trans", "gs_sym_max", "gather_sym",
+                 "gather_notrans", "gather_trans", "scatter_sym", "scatter_notrans",
+                 "scatter_trans"]
 BS_CASES = [(1, 11), (5, 12), (1000, 13), (65537, 14), (300001, 15), (1048576, 16)]
 
 
@@ -74,6 +88,34 @@ def ogs_case(nx, ny, nz, p, perm, qseed):
         print(stem, rec["N"], rec["Ngather"])
 
 
+def ogsmr_case(size, nx, ny, nz, p, qseed):
+    """The reference's ogs_t on `size` ranks (forked, MPI stand-in): per rank the box
+    ids, its signed ids after the mesh's unique flagging, the counts of a Pairwise
+    handle on those ids and digests of its operations on seeded values."""
+    with tempfile.TemporaryDirectory() as d:
+        run(["ogsmr", size, nx, ny, nz, p, qseed], d)
+        ranks, ids = [], {}
+        for r in range(size):
+            ld = lambda n, t: np.fromfile(f"{d}/r{r}_{n}.bin", dtype=t)  # noqa: E731
+            cnt = ld("counts", np.int64)
+            rec = {"counts": dict(zip(["N", "NlocalP", "NlocalT", "NhaloP", "NhaloT", "Ngather",
+                                       "NgatherGlobal", "gather_defined"], map(int, cnt))),
+                   "sha256": {"box_ids": sha(ld("box_ids", np.int64))}, "head": {}}
+            ids[f"r{r}"] = ld("ids", np.int64)
+            for name in OGSMR_OUTPUTS:
+                a = ld(name, np.float64)
+                rec["sha256"][name] = sha(a)
+                rec["head"][name] = hexes(a)
+            ranks.append(rec)
+        stem = f"ogsmr_{size}r_{nx}x{ny}x{nz}_p{p}"
+        np.savez_compressed(HERE / f"{stem}_ids.npz", **ids)
+        case = {"ranks": size, "mesh": [nx, ny, nz, p], "qseed": qseed,
+                "q_seed_of_rank": "qseed + 1000*rank", "g_seed_of_rank": "qseed + 1000*rank + 1",
+                "ids_file": f"{stem}_ids.npz", "per_rank": ranks}
+        (HERE / f"{stem}.json").write_text(json.dumps(case, indent=1) + "\n")
+        print(stem, [r["counts"]["NhaloT"] for r in ranks])
+
+
 def bs_case(n, seed):
     with tempfile.TemporaryDirectory() as d:
         run(["bs", n, seed], d)
@@ -94,6 +136,8 @@ def main():
         ogs_case(*c)
     for c in BS_CASES:
         bs_case(*c)
+    for c in OGSMR_CASES:
+        ogsmr_case(*c)
 
 
 if __name__ == "__main__":

@@ -75,6 +75,42 @@ def test_box_gather_and_scatter_fp64(cuda, orc, box):
                                                         np.zeros(ids.size)))
 
 
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("box", [(2, 2, 2, 1), (2, 2, 2, 2), (3, 2, 2, 3), (2, 1, 1, 4)])
+def test_small_plans_n_operator_every_kernel(cuda, orc, kernel, box):
+    """Plans of one warp chunk, whose N operator has the same row range as T but
+    fewer entries: every N-operator operation with every kernel variant."""
+    saved = {key: capi.tune_get(key) for key in ("ogs.kernel", "ogs.kernel.gather",
+                                                  "ogs.kernel.scatter")}
+    try:
+        capi.tune_set("ogs.kernel.gather", kernel)
+        capi.tune_set("ogs.kernel.scatter", kernel)
+        capi.tune_set("ogs.kernel", min(kernel, 3))
+        ids = O.box_hex_ids(*box)
+        h, ref = make(orc, ids)
+        n, nT, nN = ids.size, ref["rsT"].size - 1, ref["rsN"].size - 1
+        assert ref["ciN"].size < ref["ciT"].size
+        q = orc.uniform(n, 41)
+        gv = torch.zeros(max(nN, 1), dtype=torch.float64, device="cuda")
+        h.Gather(gv, torch.from_numpy(q).cuda(), 1, O.Add, O.NoTrans)
+        np.testing.assert_array_equal(host(gv)[:nN], orc.gather(ref["rsN"], ref["ciN"], q))
+        g = orc.uniform(nT, 43)
+        dv = torch.zeros(n, dtype=torch.float64, device="cuda")
+        h.Scatter(dv, torch.from_numpy(g).cuda(), 1, O.Trans)
+        np.testing.assert_array_equal(host(dv), orc.scatter(ref["rsN"], ref["ciN"], g[:nN],
+                                                            np.zeros(n)))
+        rsNp = pad(ref["rsN"], nT)
+        for trans, (grs, gci, srs, sci) in ((O.NoTrans, (rsNp, ref["ciN"], ref["rsT"], ref["ciT"])),
+                                            (O.Trans, (ref["rsT"], ref["ciT"], rsNp, ref["ciN"]))):
+            dv = torch.from_numpy(q).cuda()
+            h.GatherScatter(dv, 1, O.Add, trans)
+            np.testing.assert_array_equal(host(dv), orc.gather_scatter(grs, gci, srs, sci, q),
+                                          err_msg=f"gs trans={trans}")
+    finally:
+        for key, v in saved.items():
+            capi.tune_set(key, v)
+
+
 @pytest.mark.parametrize("tcode", [capi.FLOAT, capi.DOUBLE, capi.INT32, capi.INT64])
 @pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
 @pytest.mark.parametrize("k", [1, 3])
