@@ -69,7 +69,13 @@ void        sp_launch_count_reset(void);
  *    renumbered in that breadth-first order so that chunks are full; default 1),
  *    "ogs.page_shift" (3..16, default 9: pages of 2^9 entries) and "ogs.rows" (0
  *    CSR order, 1 rows grouped by size inside a chunk; default 1) for the warp
- *    chunks of plans created afterwards;
+ *    chunks of plans created afterwards; "ogs.ball_shift" (0 = pages visited
+ *    breadth-first over the whole mesh, 1..26 = as a chain of breadth-first balls
+ *    of 2^n entries; default 0);
+ *  "ogs.gs_order" (-1 = the gather+scatter uses the main walk; 0..2 = plans
+ *    created afterwards also hold a second walk of T in that order, used by the
+ *    in-place gather+scatter; default -1), "ogs.gs_page_shift" (3..16, default 8)
+ *    and "ogs.gs_ball_shift" (0..26, default 18) for that walk;
  *  "ogs.kernel" / "ogs.kernel.gather" / "ogs.kernel.scatter" (gather+scatter /
  *    gather / scatter): 0 block kernels, 1 warp-chunk kernels, 2 pipelined
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or

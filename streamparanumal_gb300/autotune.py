@@ -4,8 +4,10 @@ For a hex box of degree p it times BS6 (Gather Trans), BS7 (Scatter NoTrans) and
 BS8 (GatherScatter Sym) under every compiled variant -- block kernels (rows cut into
 blocks of `ogs.block_nnz` entries), warp-chunk kernels, pipelined persistent
 warp-chunk kernels and asynchronously staged ones, each with chunks in row order or
-breadth-first page order and rows in CSR order or grouped by size -- and keeps the
-fastest by total time.  Results are stored per degree in a JSON table
+breadth-first page order (whole-mesh wavefronts or chains of balls) and rows in CSR
+order or grouped by size -- and keeps the fastest by total time.  The in-place
+gather+scatter then gets its own walk of the operator when one of the candidate
+walks beats it on the chosen plan.  Results are stored per degree in a JSON table
 (`tuning/gb300.json` by default) that :func:`apply` loads into the library's tuning
 knobs before plans are built.  Every variant computes the same bits; only speed
 differs.
@@ -30,16 +32,31 @@ PLAN_CONFIGS = [{"order": 1, "rows": 1, "block_nnz": 2048}, {"order": 1, "rows":
 DEFAULT_PAGE_SHIFT = 9
 
 
+BALL_OVER_PAGE = 10  # balls of 2^(page_shift + 10) entries: about a thousand pages
+
+
 def plan_configs(p: int) -> list[dict]:
     """PLAN_CONFIGS with the default 512-entry pages, plus breadth-first pages of
     about one element ((p+1)^3 entries) when that size differs, plus the
-    renumbered breadth-first walk over element-sized pages (chunk order 2)."""
+    renumbered breadth-first walk over element-sized pages (chunk order 2); the
+    grouped breadth-first configurations also as chains of balls."""
     shift = max(3, ((p + 1) ** 3 - 1).bit_length())
-    cfgs = [dict(c, page_shift=DEFAULT_PAGE_SHIFT) for c in PLAN_CONFIGS]
+    cfgs = [dict(c, page_shift=DEFAULT_PAGE_SHIFT, ball_shift=0) for c in PLAN_CONFIGS]
     if shift != DEFAULT_PAGE_SHIFT:
-        cfgs.insert(1, {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": shift})
-    cfgs.insert(1, {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": shift})
-    return cfgs
+        cfgs.insert(1, {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": shift,
+                        "ball_shift": 0})
+    cfgs.insert(1, {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": shift, "ball_shift": 0})
+    balls = [dict(c, ball_shift=c["page_shift"] + BALL_OVER_PAGE) for c in cfgs
+             if c["order"] >= 1 and c["rows"] == 1]
+    return cfgs + balls
+
+
+def gs_walks(p: int) -> list[dict]:
+    """Candidate walks of the in-place gather+scatter: renumbered breadth-first
+    walks (chunk order 2) over pages of half and one element, whole-mesh or balls."""
+    shift = max(3, ((p + 1) ** 3 - 1).bit_length())
+    return [{"gs_order": 2, "gs_page_shift": s, "gs_ball_shift": b}
+            for s in sorted({max(3, shift - 1), shift}) for b in (0, s + BALL_OVER_PAGE)]
 KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
            3: "warp-async-staged gathers / column-order scatter",
            4: "column-order gathers / persistent prefetching column-order scatter",
@@ -61,9 +78,14 @@ def _time(fn, reps: int, stream) -> float:
 
 
 KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift",
-         "block_nnz": "ogs.block_nnz",
+         "block_nnz": "ogs.block_nnz", "ball_shift": "ogs.ball_shift",
+         "gs_order": "ogs.gs_order", "gs_page_shift": "ogs.gs_page_shift",
+         "gs_ball_shift": "ogs.gs_ball_shift",
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
          "kernel_scatter": "ogs.kernel.scatter"}
+# plan-time knobs a table entry may leave out: the library defaults
+PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1}
+GS_WALK_KERNELS = (1, 2, 5)
 
 
 def _set(cfg: dict) -> None:
@@ -98,12 +120,19 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
         ids = O.box_hex_ids(E, E, E, p, perm_seed, device="cuda")
     Nt = ids.numel() if isinstance(ids, torch.Tensor) else ids.size
     q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
-    timings = []  # (order, rows, page_shift, block_nnz, kernel, op, ms)
+    timings = []  # (order, rows, page_shift, ball_shift, block_nnz, kernel, op, ms)
+    walk_timings = []  # (gs_order, gs_page_shift, gs_ball_shift, kernel, ms)
+
+    def build():
+        h = O.ogs_t()
+        h.Setup(Nt, ids.clone() if isinstance(ids, torch.Tensor) else ids.copy(), unique=True)
+        return h
+
     try:
+        _set(PLAN_DEFAULTS)
         for pc in plan_configs(p):
             _set(pc)
-            h = O.ogs_t()
-            h.Setup(Nt, ids.clone() if isinstance(ids, torch.Tensor) else ids.copy(), unique=True)
+            h = build()
             gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
             ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
                    "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
@@ -111,32 +140,56 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
             for op, key in OPS:
                 for k in _kernels(pc, op):
                     _set({key: k})
-                    timings.append((pc["order"], pc["rows"], pc["page_shift"], pc["block_nnz"], k,
-                                    op, _time(ops[op], reps, stream)))
+                    timings.append((pc["order"], pc["rows"], pc["page_shift"], pc["ball_shift"],
+                                    pc["block_nnz"], k, op, _time(ops[op], reps, stream)))
             h.Free()
             del gq
+        best_total, best, best_gs_ms = None, None, None
+        for layout in sorted({t[:4] for t in timings}):
+            order, rows, shift, ball = layout
+            choice = {"order": order, "rows": rows, "page_shift": shift, "ball_shift": ball}
+            total, gs_ms = 0.0, None
+            for op, key in OPS:
+                # block kernels and the column-major scatter do not depend on the chunk
+                # layout, so they compete under every plan configuration
+                cands = [t for t in timings if t[6] == op and (
+                    t[:4] == layout or t[5] == 0 or (op == "BS7" and t[5] == 5))]
+                *_, bnnz, k, _, ms = min(cands, key=lambda t: t[7])
+                choice[key] = k
+                if k == 0:
+                    choice["block_nnz"] = bnnz
+                total += ms
+                if op == "BS8":
+                    gs_ms = ms
+            if best_total is None or total < best_total:
+                best_total, best, best_gs_ms = total, choice, gs_ms
+        best.setdefault("block_nnz", 2048)
+        # a walk of its own for the gather+scatter, on the chosen plan
+        if best["order"] != 0 or best["rows"] != 0 or best.get("kernel_gs", 0) != 0:
+            for w in gs_walks(p):
+                _set({**best, **w})
+                h = build()
+                for k in GS_WALK_KERNELS:
+                    _set({"kernel_gs": k})
+                    walk_timings.append((w["gs_order"], w["gs_page_shift"], w["gs_ball_shift"], k,
+                                         _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), reps,
+                                               stream)))
+                h.Free()
+        best["gs_order"] = -1
+        if walk_timings:
+            go, gp, gb, k, ms = min(walk_timings, key=lambda t: t[4])
+            if ms < best_gs_ms:
+                best.update(gs_order=go, gs_page_shift=gp, gs_ball_shift=gb, kernel_gs=k)
+                best_total += ms - best_gs_ms
     finally:
         _set(saved)
-    best_total, best = None, None
-    for order, rows, shift in sorted({t[:3] for t in timings}):
-        choice, total = {"order": order, "rows": rows, "page_shift": shift}, 0.0
-        for op, key in OPS:
-            # block kernels and the column-major scatter do not depend on the chunk
-            # layout, so they compete under every plan configuration
-            cands = [t for t in timings if t[5] == op and (
-                t[:3] == (order, rows, shift) or t[4] == 0 or (op == "BS7" and t[4] == 5))]
-            _, _, _, bnnz, k, _, ms = min(cands, key=lambda t: t[6])
-            choice[key] = k
-            if k == 0:
-                choice["block_nnz"] = bnnz
-            total += ms
-        if best_total is None or total < best_total:
-            best_total, best = total, choice
-    best.setdefault("block_nnz", 2048)
     return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,
             "best_total_ms": best_total,
-            "candidates": [{"order": o, "rows": r, "page_shift": ps, "block_nnz": b, "kernel": k,
-                            "op": op, "ms": ms} for o, r, ps, b, k, op, ms in timings]}
+            "candidates": [{"order": o, "rows": r, "page_shift": ps, "ball_shift": bs,
+                            "block_nnz": b, "kernel": k, "op": op, "ms": ms}
+                           for o, r, ps, bs, b, k, op, ms in timings],
+            "gs_walks": [{"gs_order": o, "gs_page_shift": ps, "gs_ball_shift": bs, "kernel": k,
+                          "ms": ms} for o, ps, bs, k, ms in walk_timings]}
 
 
 def load_table(path: Path = TABLE) -> dict:
@@ -174,5 +227,5 @@ def apply(p: int, perm: bool = False, table: dict | None = None) -> dict:
     table = load_table() if table is None else table
     cfg = table.get(f"p{p}" + ("_perm" if perm else "")) or table.get(f"p{p}")
     if cfg:
-        _set(cfg)
+        _set({**PLAN_DEFAULTS, **cfg})
     return cfg or {}

@@ -49,6 +49,10 @@ enum TuneKey : int {
   kTuneOgsKernelScatter,    // ogs scatter: kernel variant as kTuneOgsKernel
   kTuneOgsRows,             // ogs plan: rows inside a warp chunk, 0 = CSR order, 1 = grouped by size
   kTuneOgsPageShift,        // ogs plan: log2 of the page size of the breadth-first chunk order
+  kTuneOgsBallShift,        // ogs plan: 0 breadth-first pages, else balls of 2^n entries
+  kTuneOgsGsOrder,          // ogs plan: -1 gather+scatter on the main walk, else its own walk's order
+  kTuneOgsGsPageShift,      // ogs plan: page size of the gather+scatter walk
+  kTuneOgsGsBallShift,      // ogs plan: ball size of the gather+scatter walk
   kTuneCount
 };
 int64_t tune(TuneKey k);

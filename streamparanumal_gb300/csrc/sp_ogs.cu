@@ -851,6 +851,14 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
                    p->d_colIdsST, p->d_e2sT, p->d_permT};
 }
+// The gather+scatter walk when the plan has one (kernels 3 and 4 need the column
+// order arrays of the main walk, so they run as kernel 2 there).
+static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
+  const int32_t* rs = p->d_rsGS ? p->d_rsGS : p->d_rowStartsT;
+  const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
+  return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
+                   p->gs_grouped, nullptr, nullptr, nullptr};
+}
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
                    p->d_colIdsN, 0, nullptr, nullptr, nullptr};
@@ -901,7 +909,9 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
   const int kv = variant(kTuneOgsKernel, K, p->nchunksT);
-  if ((trans == SP_SYM || p->n_is_t) && kv > 0) {
+  if ((trans == SP_SYM || p->n_is_t) && kv > 0 && p->nchunksGS > 0) {
+    launch_chunked_gather<T, OP, 0>((kv == 3 || kv == 4) ? 2 : kv, chunks_gs(p), v, nullptr, s);
+  } else if ((trans == SP_SYM || p->n_is_t) && kv > 0) {
     launch_chunked_gather<T, OP, 0>(kv, chunks_t(p), v, nullptr, s);
   } else if (trans == SP_SYM || p->n_is_t) {
     k_ogs_gs_sym<T, OP><<<grid, kOgsThreads, 0, s>>>(p->d_blocksT, p->d_rowStartsT, p->d_colIdsT,
@@ -1096,6 +1106,11 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->d_walkRsT = p->d_walkCiT = p->d_permT = nullptr;
   if (p->d_rowOfColT) cudaFree(p->d_rowOfColT);
   p->d_rowOfColT = nullptr;
+  if (p->d_chunksGS) cudaFree(p->d_chunksGS);
+  if (p->d_rsGS) cudaFree(p->d_rsGS);
+  if (p->d_ciGS) cudaFree(p->d_ciGS);
+  p->d_chunksGS = p->d_rsGS = p->d_ciGS = nullptr;
+  p->nchunksGS = p->gs_grouped = 0;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1120,6 +1135,58 @@ static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
 }
 
 // Finishes a plan whose host CSR arrays are filled: validation, partition, upload.
+// The gather+scatter walk (knob ogs.gs_order >= 0): a second chunking of T in its
+// own order (pages of 2^ogs.gs_page_shift entries, balls of 2^ogs.gs_ball_shift),
+// with rows grouped by size when ogs.rows is 1.  The in-place gather+scatter then
+// need not share the walk that suits the gathers (measured on the permuted 64^3
+// p=7 box: gathers fastest on breadth-first pages of 512 entries, gather+scatter on
+// a renumbered walk of 256-entry pages in balls of 2^18 entries).
+static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
+  const int order = (int)tune(kTuneOgsGsOrder);
+  if (order < 0 || p->nchunksT == 0) return SP_SUCCESS;
+  const int shift = (int)tune(kTuneOgsGsPageShift), ball = (int)tune(kTuneOgsGsBallShift);
+  std::vector<int32_t> perm, walkRs, walkCi, pairs;
+  const int32_t* wrs = p->rowStartsT.data();
+  const int32_t* wci = p->colIdsT.data();
+  if (order == 2) {
+    bfs_row_sequence(p->NrowsT, wrs, wci, p->N, shift, ball, perm);
+    walkRs.assign((size_t)p->NrowsT + 1, 0);
+    for (int32_t k = 0; k < p->NrowsT; ++k)
+      walkRs[k + 1] = walkRs[k] + (p->rowStartsT[perm[k] + 1] - p->rowStartsT[perm[k]]);
+    walkCi.resize(p->nnzT);
+#pragma omp parallel for schedule(static)
+    for (int32_t k = 0; k < p->NrowsT; ++k)
+      std::copy(p->colIdsT.begin() + p->rowStartsT[perm[k]],
+                p->colIdsT.begin() + p->rowStartsT[perm[k] + 1], walkCi.begin() + walkRs[k]);
+    wrs = walkRs.data();
+    wci = walkCi.data();
+  }
+  if (!build_chunks(p->NrowsT, wrs, wci, p->N, order == 2 ? 0 : order, pairs, shift, ball))
+    return SP_SUCCESS;
+  std::vector<int32_t> quads(pairs.size() * 2);
+  for (size_t c = 0; c < pairs.size() / 2; ++c) {
+    quads[4 * c + 0] = pairs[2 * c];
+    quads[4 * c + 1] = pairs[2 * c + 1];
+    quads[4 * c + 2] = wrs[pairs[2 * c]];
+    quads[4 * c + 3] = wrs[pairs[2 * c + 1]];
+  }
+  sp_status st;
+  if ((st = upload(quads, &p->d_chunksGS, s))) return st;
+  if (tune(kTuneOgsRows) == 1) {
+    std::vector<int32_t> rowsG, colIdsG;
+    build_grouped(quads, p->NrowsT, wrs, wci, rowsG, colIdsG);
+    if ((st = upload(rowsG, &p->d_rsGS, s))) return st;
+    if ((st = upload(colIdsG, &p->d_ciGS, s))) return st;
+    p->gs_grouped = 1;
+  } else if (order == 2) {
+    if ((st = upload(walkRs, &p->d_rsGS, s))) return st;
+    if ((st = upload(walkCi, &p->d_ciGS, s))) return st;
+  }
+  p->nchunksGS = (int32_t)(quads.size() / 4);
+  SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+  return SP_SUCCESS;
+}
+
 sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
   int32_t maxRow = 0;
   sp_status st = validate_csr(p->N, p->NrowsT, p->rowStartsT.data(), p->colIdsT.data(), "T",
@@ -1219,6 +1286,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
   // element numbering; perm maps a walk row back to its row of T.
   p->chunk_order = (int32_t)tune(kTuneOgsOrder);
   const int page_shift = (int)tune(kTuneOgsPageShift);
+  const int ball_shift = (int)tune(kTuneOgsBallShift);
   const bool renumber = p->chunk_order == 2;
   std::vector<int32_t> walkRs, walkCi, perm;
   const int32_t* wrs = p->rowStartsT.data();
@@ -1232,7 +1300,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       if (p->rowStartsT[r + 1] - p->rowStartsT[r] > kWarpChunkNnz) tooBig = 1;
     fits = !tooBig;
     if (fits) {
-      bfs_row_sequence(p->NrowsT, wrs, wci, p->N, page_shift, perm);
+      bfs_row_sequence(p->NrowsT, wrs, wci, p->N, page_shift, ball_shift, perm);
       walkRs.assign((size_t)p->NrowsT + 1, 0);
       for (int32_t k = 0; k < p->NrowsT; ++k)
         walkRs[k + 1] = walkRs[k] + (p->rowStartsT[perm[k] + 1] - p->rowStartsT[perm[k]]);
@@ -1243,13 +1311,14 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
                   p->colIdsT.begin() + p->rowStartsT[perm[k] + 1], walkCi.begin() + walkRs[k]);
       wrs = walkRs.data();
       wci = walkCi.data();
-      fits = build_chunks(p->NrowsT, wrs, wci, p->N, 0, chunksT, page_shift);
+      fits = build_chunks(p->NrowsT, wrs, wci, p->N, 0, chunksT, page_shift, ball_shift);
     }
   } else {
-    fits = build_chunks(p->NrowsT, wrs, wci, p->N, p->chunk_order, chunksT, page_shift);
+    fits = build_chunks(p->NrowsT, wrs, wci, p->N, p->chunk_order, chunksT, page_shift,
+                        ball_shift);
   }
   if (fits && build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, 0, chunksN,
-                           page_shift)) {
+                           page_shift, 0)) {
     p->nchunksT = (int32_t)(chunksT.size() / 2);
     p->nchunksN = (int32_t)(chunksN.size() / 2);
     // descriptors (r0, r1, g0, g1): the entry range rides along with the row range
@@ -1302,6 +1371,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     for (int32_t r = 0; r < p->NrowsT; ++r)
       for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) rowOfCol[p->colIdsT[i]] = r;
     if ((st = upload(rowOfCol, &p->d_rowOfColT, s))) return st;
+    if ((st = build_gs_walk(p, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   } else {
     p->nchunksT = p->nchunksN = 0;

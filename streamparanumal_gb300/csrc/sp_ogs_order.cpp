@@ -12,7 +12,8 @@
 //     together in time, so the data one chunk touches in a neighbouring page is
 //     usually still in L2 when that page's own chunks run -- whatever the element
 //     numbering in memory.  A page of about one element's nodes makes the visit a
-//     wavefront over the mesh.
+//     wavefront over the mesh.  With ball_shift > 0 the pages are visited as a
+//     chain of breadth-first balls of 2^ball_shift entries instead (page_order).
 #include <parallel/algorithm>
 
 #include <algorithm>
@@ -75,7 +76,7 @@ struct PageOrder {
 };
 
 static void page_order(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols,
-                       int page_shift, PageOrder& po) {
+                       int page_shift, int ball_shift, PageOrder& po) {
   const int64_t npages64 = ((int64_t)std::max(ncols, 1) + (1LL << page_shift) - 1) >> page_shift;
   const int32_t npages = (int32_t)npages64;
   po.npages = npages;
@@ -191,11 +192,54 @@ static void page_order(int32_t nrows, const int32_t* rs, const int32_t* ci, int3
     std::sort(b, e);
     adjEnd[p] = std::unique(b, e) - adj.data();
   }
-  // breadth-first page order, restarting at the lowest unvisited page
   std::vector<uint8_t> seen(npages, 0);
   std::vector<int32_t>& queue = po.queue;
   queue.clear();
   queue.reserve(npages);
+  if (ball_shift > 0) {
+    // balls: breadth-first from a seed until the ball holds 2^ball_shift entries,
+    // each next seed an unvisited neighbour of the most recent ball's rim (else the
+    // lowest unvisited page).  The walk then moves through the mesh as a chain of
+    // compact regions, so a page's neighbours are visited within a few balls of it
+    // instead of one breadth-first shell (a whole cross-section of the mesh) away.
+    const int64_t cap = std::max<int64_t>(1, (int64_t)1 << std::max(0, ball_shift - page_shift));
+    std::vector<int32_t> rim;  // pages of finished balls whose neighbours were not all taken
+    int32_t low = 0;
+    while ((int64_t)queue.size() < npages) {
+      int32_t seed = -1;
+      while (seed < 0 && !rim.empty()) {
+        const int32_t p = rim.back();
+        bool open = false;
+        for (int64_t k = adjStart[p]; k < adjEnd[p] && seed < 0; ++k)
+          if (!seen[adj[k]]) seed = adj[k];
+        for (int64_t k = adjStart[p]; k < adjEnd[p] && !open; ++k)
+          if (!seen[adj[k]] && adj[k] != seed) open = true;
+        if (!open) rim.pop_back();
+      }
+      if (seed < 0) {
+        while (seen[low]) ++low;
+        seed = low;
+      }
+      const size_t b0 = queue.size();
+      seen[seed] = 1;
+      queue.push_back(seed);
+      size_t head = b0;
+      while (head < queue.size() && (int64_t)(queue.size() - b0) < cap) {
+        const int32_t p = queue[head++];
+        for (int64_t k = adjStart[p]; k < adjEnd[p] && (int64_t)(queue.size() - b0) < cap; ++k) {
+          const int32_t q = adj[k];
+          if (!seen[q]) {
+            seen[q] = 1;
+            queue.push_back(q);
+          }
+        }
+      }
+      // the ball's rim: pages whose neighbours may still be unvisited
+      for (size_t k = (head > b0 ? head - 1 : b0); k < queue.size(); ++k) rim.push_back(queue[k]);
+    }
+    return;
+  }
+  // breadth-first page order, restarting at the lowest unvisited page
   for (int32_t start = 0; start < npages; ++start) {
     if (seen[start]) continue;
     seen[start] = 1;
@@ -215,7 +259,7 @@ static void page_order(int32_t nrows, const int32_t* rs, const int32_t* ci, int3
 }
 
 bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols, int order,
-                  std::vector<int32_t>& chunks, int page_shift) {
+                  std::vector<int32_t>& chunks, int page_shift, int ball_shift) {
   chunks.clear();
   int32_t tooBig = 0;
 #pragma omp parallel for schedule(static) reduction(max : tooBig)
@@ -228,7 +272,7 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
     return true;
   }
   PageOrder po;
-  page_order(nrows, rs, ci, ncols, page_shift, po);
+  page_order(nrows, rs, ci, ncols, page_shift, ball_shift, po);
   const int32_t npages = po.npages, nonEmpty = po.nonEmpty;
   const std::vector<int32_t>& rowPage = po.rowPage;
   const std::vector<int32_t>& pageRows = po.pageRows;
@@ -271,11 +315,11 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
 }
 
 void bfs_row_sequence(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols,
-                      int page_shift, std::vector<int32_t>& seq) {
+                      int page_shift, int ball_shift, std::vector<int32_t>& seq) {
   seq.clear();
   if (nrows == 0) return;
   PageOrder po;
-  page_order(nrows, rs, ci, ncols, page_shift, po);
+  page_order(nrows, rs, ci, ncols, page_shift, ball_shift, po);
   seq.resize(nrows);
   std::vector<int64_t> at(po.npages + 1, 0);
   for (int32_t k = 0; k < po.npages; ++k) {

@@ -44,15 +44,16 @@ bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t
 
 // Cuts rows [0, nrows) into warp chunks, stored as (first row, end row) pairs in the
 // order they are scheduled: 0 = row order, 1 = breadth-first over pages of
-// 2^page_shift local entries.  Returns false when a row holds more than
-// kWarpChunkNnz entries.
+// 2^page_shift local entries (ball_shift > 0: a chain of breadth-first balls of
+// 2^ball_shift entries).  Returns false when a row holds more than kWarpChunkNnz
+// entries.
 bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
-                  int order, std::vector<int32_t>& chunks, int page_shift);
+                  int order, std::vector<int32_t>& chunks, int page_shift, int ball_shift);
 
 // All rows in breadth-first page order: each page's rows (ascending) as the pages
 // are visited, then rows without members.  seq[k] = the k-th row of the walk.
 void bfs_row_sequence(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds,
-                      int32_t ncols, int page_shift, std::vector<int32_t>& seq);
+                      int32_t ncols, int page_shift, int ball_shift, std::vector<int32_t>& seq);
 
 // Rows of every chunk regrouped by size.  `quads` holds the chunk descriptors
 // (r0, r1, g0, g1).  Inside chunk [r0, r1) the rows are reordered by member count,
@@ -143,6 +144,13 @@ struct sp_ogs_plan {
   // the row of T holding each local column (-1: in no row), for the column-major
   // scatter; built with the warp chunks
   int32_t* d_rowOfColT = nullptr;    // N
+  // optional second walk of T for the in-place gather+scatter (knob ogs.gs_order):
+  // its own chunk order, page and ball sizes, rows grouped by size or the walk CSR
+  int32_t* d_chunksGS = nullptr;
+  int32_t nchunksGS = 0;
+  int32_t gs_grouped = 0;
+  int32_t* d_rsGS = nullptr;         // grouped rows, or the walk's row starts
+  int32_t* d_ciGS = nullptr;         // grouped or walk column ids
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
   bool own_blocks_n = false;      // d_blocksN is a separate allocation
 

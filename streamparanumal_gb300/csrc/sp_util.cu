@@ -40,6 +40,10 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.kernel.scatter", 0, 5, {5}},
     {"ogs.rows", 0, 1, {1}},
     {"ogs.page_shift", 3, 16, {9}},
+    {"ogs.ball_shift", 0, 26, {0}},
+    {"ogs.gs_order", -1, 2, {-1}},
+    {"ogs.gs_page_shift", 3, 16, {8}},
+    {"ogs.gs_ball_shift", 0, 26, {18}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

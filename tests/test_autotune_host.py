@@ -5,19 +5,30 @@ import json
 from streamparanumal_gb300 import autotune
 
 
-def test_plan_configs_add_element_pages_and_renumbered_walk():
+def test_plan_configs_add_element_pages_renumbered_walk_and_balls():
     # p = 7: an element is 512 entries, the default page size
     cfgs = autotune.plan_configs(7)
-    assert {(c["order"], c["rows"], c["page_shift"]) for c in cfgs} >= {
-        (1, 1, 9), (2, 1, 9), (1, 0, 9), (0, 1, 9), (0, 0, 9)}
-    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 1
-    # p = 3: 64-entry elements add pages of 2^6 for both breadth-first orders
+    assert {(c["order"], c["rows"], c["page_shift"], c["ball_shift"]) for c in cfgs} >= {
+        (1, 1, 9, 0), (2, 1, 9, 0), (1, 0, 9, 0), (0, 1, 9, 0), (0, 0, 9, 0), (1, 1, 9, 19),
+        (2, 1, 9, 19)}
+    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 1 + 2
+    # p = 3: 64-entry elements add pages of 2^6 for both breadth-first orders, and
+    # every grouped breadth-first layout also runs as a chain of balls
     cfgs = autotune.plan_configs(3)
-    assert {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": 6} in cfgs
-    assert {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": 6} in cfgs
-    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 2
+    assert {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": 6, "ball_shift": 0} in cfgs
+    assert {"order": 2, "rows": 1, "block_nnz": 2048, "page_shift": 6, "ball_shift": 16} in cfgs
+    assert len(cfgs) == len(autotune.PLAN_CONFIGS) + 2 + 3
     # p = 1: 8-entry elements
     assert min(c["page_shift"] for c in autotune.plan_configs(1)) == 3
+
+
+def test_gather_scatter_walk_candidates():
+    assert autotune.gs_walks(7) == [
+        {"gs_order": 2, "gs_page_shift": 8, "gs_ball_shift": 0},
+        {"gs_order": 2, "gs_page_shift": 8, "gs_ball_shift": 18},
+        {"gs_order": 2, "gs_page_shift": 9, "gs_ball_shift": 0},
+        {"gs_order": 2, "gs_page_shift": 9, "gs_ball_shift": 19}]
+    assert {w["gs_page_shift"] for w in autotune.gs_walks(1)} == {3}
 
 
 def test_kernel_candidates():

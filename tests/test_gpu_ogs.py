@@ -301,6 +301,51 @@ def test_variants_types_ops(cuda, orc, kernel, rows, dtype, op):
             capi.tune_set(k, v)
 
 
+@pytest.mark.parametrize("knobs", [
+    {"ogs.order": 1, "ogs.ball_shift": 12},
+    {"ogs.order": 2, "ogs.page_shift": 6, "ogs.ball_shift": 10},
+    {"ogs.order": 1, "ogs.gs_order": 2, "ogs.gs_page_shift": 8, "ogs.gs_ball_shift": 0},
+    {"ogs.order": 0, "ogs.gs_order": 2, "ogs.gs_page_shift": 5, "ogs.gs_ball_shift": 11},
+    {"ogs.order": 2, "ogs.rows": 0, "ogs.gs_order": 1, "ogs.gs_page_shift": 6,
+     "ogs.gs_ball_shift": 14},
+    {"ogs.order": 1, "ogs.rows": 0, "ogs.gs_order": 2, "ogs.gs_page_shift": 4,
+     "ogs.gs_ball_shift": 0, "ogs.kernel": 5},
+    {"ogs.order": 1, "ogs.gs_order": 0, "ogs.kernel": 1}])
+@pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5)])
+def test_ball_chains_and_gather_scatter_walks(cuda, orc, knobs, box):
+    """Chains of balls for the main walk, and a second walk for the in-place
+    gather+scatter: every operation stays bit-exact."""
+    names = ["ogs.order", "ogs.rows", "ogs.page_shift", "ogs.ball_shift", "ogs.gs_order",
+             "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.kernel"]
+    saved = {n: capi.tune_get(n) for n in names}
+    try:
+        for n, v in knobs.items():
+            capi.tune_set(n, v)
+        nx, ny, nz, p, seed = box
+        ids = O.box_hex_ids(nx, ny, nz, p, seed)
+        h, ref = make(orc, ids)
+        q = orc.uniform(ids.size, 61)
+        for op in (O.Add, O.Max):
+            dq = torch.from_numpy(q).cuda()
+            h.GatherScatter(dq, 1, op, O.Sym)
+            np.testing.assert_array_equal(
+                host(dq), orc.gather_scatter(ref["rsT"], ref["ciT"], ref["rsT"], ref["ciT"], q, 1,
+                                             op), err_msg=f"gs op={op}")
+        ng = ref["rsT"].size - 1
+        gq = torch.zeros(ng, dtype=torch.float64, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(ref["rsT"], ref["ciT"], q))
+        nT = ng
+        rsNp = pad(ref["rsN"], nT)
+        dq = torch.from_numpy(q).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.NoTrans)
+        np.testing.assert_array_equal(
+            host(dq), orc.gather_scatter(rsNp, ref["ciN"], ref["rsT"], ref["ciT"], q))
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
+
+
 @pytest.mark.parametrize("shift", [3, 6, 12])
 @pytest.mark.parametrize("order", [1, 2])
 def test_page_sizes_of_breadth_first_order(cuda, orc, shift, order):
