@@ -285,7 +285,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
 
     from oracle import oracle as orc  # input generation only (seeded uniform values)
-    from streamparanumal_gb300 import _build, capi, kernels
+    from streamparanumal_gb300 import _build, autotune, capi, kernels
     from streamparanumal_gb300 import ogs as O
 
     _build.build_library()
@@ -301,8 +301,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     t_setup = time.time()
     h_a = torch.from_numpy(orc.uniform(N, args.seed)).pin_memory()
     h_b = torch.from_numpy(orc.uniform(N, args.seed + 1)).pin_memory()
-    # mesh ids and the gather-scatter plan, both built on the device
+    # mesh ids and the gather-scatter plan, both built on the device, with the
+    # per-degree tuning of this layout (as the BS6-BS8 drivers apply it)
     t_plan = time.time()
+    tuning = autotune.apply(p, args.perm_seed != 0)
     ids = O.box_hex_ids(mesh, mesh, mesh, p, args.perm_seed, device=dev, stream=stream)
     Nt = ids.numel()
     h = O.ogs_t()
@@ -519,7 +521,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "clocks": clocks,
         "detail": {"per_kernel": detail, "bs0_us_per_launch": bs0,
                    "storage_forms": forms, "setup_s": round(t_setup, 2),
-                   "mesh_and_plan_s": round(t_plan, 2)},
+                   "mesh_and_plan_s": round(t_plan, 2), "ogs_tuning": tuning},
     }
     if not args.no_cpu_baseline:
         gbs, desc, cores, _, _ = cpu_sample(args.cpu_nlog2, args.cpu_mesh, p, args.perm_seed,
