@@ -144,11 +144,13 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                                     pc["block_nnz"], k, op, _time(ops[op], reps, stream)))
             h.Free()
             del gq
-        best_total, best, best_gs_ms = None, None, None
+        # the main walk serves the gathers and scatters; the gather+scatter may get
+        # a walk of its own below, so it decides the main walk only on a tie
+        best_key, best, best_gs_ms = None, None, None
         for layout in sorted({t[:4] for t in timings}):
             order, rows, shift, ball = layout
             choice = {"order": order, "rows": rows, "page_shift": shift, "ball_shift": ball}
-            total, gs_ms = 0.0, None
+            main, gs_ms = 0.0, None
             for op, key in OPS:
                 # block kernels and the column-major scatter do not depend on the chunk
                 # layout, so they compete under every plan configuration
@@ -156,14 +158,16 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                     t[:4] == layout or t[5] == 0 or (op == "BS7" and t[5] == 5))]
                 *_, bnnz, k, _, ms = min(cands, key=lambda t: t[7])
                 choice[key] = k
-                if k == 0:
+                if k == 0 and (op != "BS8" or "block_nnz" not in choice):
                     choice["block_nnz"] = bnnz
-                total += ms
                 if op == "BS8":
                     gs_ms = ms
-            if best_total is None or total < best_total:
-                best_total, best, best_gs_ms = total, choice, gs_ms
+                else:
+                    main += ms
+            if best_key is None or (main, gs_ms) < best_key:
+                best_key, best, best_gs_ms = (main, gs_ms), choice, gs_ms
         best.setdefault("block_nnz", 2048)
+        best_total = best_key[0] + best_gs_ms
         # a walk of its own for the gather+scatter, on the chosen plan
         if best["order"] != 0 or best["rows"] != 0 or best.get("kernel_gs", 0) != 0:
             for w in gs_walks(p):
