@@ -85,7 +85,7 @@ KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift
          "kernel_scatter": "ogs.kernel.scatter"}
 # plan-time knobs a table entry may leave out: the library defaults
 PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1}
-GS_WALK_KERNELS = (1, 2, 5)
+GS_WALK_KERNELS = (1, 2, 3, 5)
 
 
 def _set(cfg: dict) -> None:

@@ -851,8 +851,8 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
                    p->d_colIdsST, p->d_e2sT, p->d_permT};
 }
-// The gather+scatter walk when the plan has one (kernels 3 and 4 need the column
-// order arrays of the main walk, so they run as kernel 2 there).
+// The gather+scatter walk when the plan has one (kernel 4 needs the column-order
+// arrays of the main walk, so it runs as kernel 2 there).
 static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   const int32_t* rs = p->d_rsGS ? p->d_rsGS : p->d_rowStartsT;
   const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
@@ -910,7 +910,7 @@ static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cud
   dim3 grid(p->NrowBlocksT, K);
   const int kv = variant(kTuneOgsKernel, K, p->nchunksT);
   if ((trans == SP_SYM || p->n_is_t) && kv > 0 && p->nchunksGS > 0) {
-    launch_chunked_gather<T, OP, 0>((kv == 3 || kv == 4) ? 2 : kv, chunks_gs(p), v, nullptr, s);
+    launch_chunked_gather<T, OP, 0>(kv, chunks_gs(p), v, nullptr, s);  // 4 runs as 2 here
   } else if ((trans == SP_SYM || p->n_is_t) && kv > 0) {
     launch_chunked_gather<T, OP, 0>(kv, chunks_t(p), v, nullptr, s);
   } else if (trans == SP_SYM || p->n_is_t) {

@@ -21,9 +21,9 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
         # plus the three breadth-first ones as chains of balls) x (5 + 4 + 5) kernels,
         # the breadth-first CSR plan x (5 + 2 + 5), the row-order CSR plan with block
         # kernels and the column-major scatter too (6 + 4 + 6), and block kernels at
-        # block_nnz 1024 (3); then the gather+scatter walks x 3 kernels
+        # block_nnz 1024 (3); then the gather+scatter walks x their kernels
         assert len(res["candidates"]) == 98 + 12 + 16 + 3
-        assert len(res["gs_walks"]) in (0, 3 * len(autotune.gs_walks(3)))
+        assert len(res["gs_walks"]) in (0, len(autotune.GS_WALK_KERNELS) * len(autotune.gs_walks(3)))
         table = {}
         autotune.record(table, res)
         path = tmp_path / "t.json"
