@@ -160,3 +160,24 @@ def test_gpu_multi_rank_device_ids_and_start_finish(cuda, orc):
                                                        O.Add, O.Sym, ex[c.rank]))
     for r in range(P):
         np.testing.assert_array_equal(got[r], want[r])
+
+
+def test_gpu_ranks_without_nodes_or_ids(cuda, orc):
+    P = 3
+    rng = np.random.default_rng(2)
+    ids = [rng.integers(1, 50, 40).astype(np.int64), np.zeros(0, np.int64),
+           np.zeros(10, np.int64)]
+    hs = setup_ranks(ids, unique=True)
+    views = [M.FromOgs(o) for o, _ in hs]
+    vals = [rng.standard_normal(o.N) for o, _ in hs]
+
+    def gs(o, s, r):
+        v = torch.from_numpy(vals[r]).cuda()
+        o.GatherScatter(v, 1, O.Add, O.Sym, stream=s)
+        return v.cpu().numpy()
+    got = on_ranks(hs, gs)
+    ex = M.thread_exchanges(P)
+    want = C.run_threads(P, lambda c: M.gather_scatter(views[c.rank], orc, vals[c.rank], 1,
+                                                       O.Add, O.Sym, ex[c.rank]))
+    for r in range(P):
+        np.testing.assert_array_equal(got[r], want[r])

@@ -280,3 +280,22 @@ def test_gloo_ranks_match_the_reference(lib):
     for r in range(world):
         for name in ("sym", "notrans", "trans"):
             assert out[r][name] == case["per_rank"][r]["sha256"]["gs_" + name], (r, name)
+
+
+def test_ranks_without_nodes_or_ids(lib, orc):
+    """A rank with no local nodes and one whose ids are all zero take part in every
+    collective and get empty operators; the others are unaffected."""
+    P = 3
+    rng = np.random.default_rng(2)
+    ids = [rng.integers(1, 50, 40).astype(np.int64), np.zeros(0, np.int64),
+           np.zeros(10, np.int64)]
+    ids[0][::3] *= -1
+    hh = C.run_threads(P, lambda c: M.HostHandle(ids[c.rank].size, ids[c.rank], c, capi.SIGNED,
+                                                 True))
+    try:
+        assert [(h.N, h.NlocalT, h.NhaloT) for h in hh][1:] == [(0, 0, 0), (10, 0, 0)]
+        assert {h.info.NgatherGlobal for h in hh} == {np.unique(np.abs(ids[0])).size}
+        _global_check(orc, ids, hh, P, np.int64)
+    finally:
+        for h in hh:
+            h.close()
