@@ -550,8 +550,8 @@ def _time(fn, stream, reps=10, warm=3) -> float:
 
 
 def storage_forms(stream, dev, h_a, h_b, h_q, h, N, Nt, Ng, per, alpha, beta) -> dict:
-    """FP32-storage forms of BS1-BS8 and the full CG update (x += alpha p,
-    r -= alpha Ap, r.r), each against its FP64 form: device time, useful GB/s (the
+    """FP32-storage forms of BS1-BS8 (BS5 as the single-launch reference update) and
+    the full CG update (x += alpha p, r -= alpha Ap, r.r), each against its FP64 form: device time, useful GB/s (the
     FP64 byte accounting / time), bytes actually moved, and the error of every
     result against the FP64 computation on the same FP64 inputs."""
     import torch
@@ -623,6 +623,22 @@ def storage_forms(stream, dev, h_a, h_b, h_q, h, N, Nt, Ng, per, alpha, beta) ->
         per["CG"] = ms64
         form("CG", ms32, 24 * N, {"rdotr_rel_err_vs_fp64": abs(r[7] - r[6]) / abs(r[6]),
                                   "x_max_rel_err_vs_fp64": xerr})
+        # the reference's BS5 update (r += alpha Ap, r.r) stored in FP32, one launch,
+        # against the order-exact FP64 BS5 of the suite
+        f64["BS5"] = 24 * N
+        r5, Ap5 = b.clone(), a.flip(0).contiguous()
+        call("sp_cg_update_ref_f64", N, cg_alpha, Ap5.data_ptr(), r5.data_ptr(),
+             res.data_ptr() + 48, sc.ptr, sptr)
+        r5_32, Ap5_32 = b.float(), Ap5.float()
+        call("sp_cg_update_ref_f32", N, cg_alpha, Ap5_32.data_ptr(), r5_32.data_ptr(),
+             res.data_ptr() + 56, sc.ptr, sptr)
+        r = res.cpu().tolist()
+        r5err = float(((r5_32.double() - r5).abs().max() / r5.abs().max()))
+        ms5 = _time(lambda: call("sp_cg_update_ref_f32", N, 1e-12, Ap5_32.data_ptr(),
+                                 r5_32.data_ptr(), res.data_ptr() + 56, sc.ptr, sptr), stream)
+        form("BS5", ms5, 12 * N, {"rdotr_rel_err_vs_fp64": abs(r[7] - r[6]) / abs(r[6]),
+                                  "r_max_rel_err_vs_fp64": r5err})
+        del r5, Ap5, r5_32, Ap5_32
         del x, rr, p_, Ap, x32, r32, p32, Ap32, a, b, a32, b32, y32
         # BS6-BS8 on FP32 node data (same plan)
         q = h_q.to(dev, non_blocking=True)

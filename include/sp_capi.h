@@ -187,6 +187,14 @@ sp_status sp_cg_update_f64(int64_t n, double alpha, const double* p, const doubl
 sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float* Ap,
                            float* x, float* r, double* rdotr, void* scratch,
                            sp_stream_t stream);
+/* The reference's BS5 update (BS/BS5/okl/bs5.okl:27-106) in one launch over the
+ * fixed grid of the fast reductions: r = fma(alpha, Ap, r) (FP32: fmaf with alpha
+ * rounded to FP32), rdotr[0] = sum r*r (FP64: deterministic, not the reference's
+ * order; FP32: compensated FP32 lanes, FP64 finish).  Scratch rules as above. */
+sp_status sp_cg_update_ref_f64(int64_t n, double alpha, const double* Ap, double* r,
+                               double* rdotr, void* scratch, sp_stream_t stream);
+sp_status sp_cg_update_ref_f32(int64_t n, double alpha, const float* Ap, float* r,
+                               double* rdotr, void* scratch, sp_stream_t stream);
 
 /* ---------------------------------------------------------------- ogs
  * A gather-scatter plan is the device form of the reference's local

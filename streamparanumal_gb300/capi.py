@@ -96,6 +96,8 @@ SIGNATURES = {
     "sp_dot_f32": (c_int32, [c_int64, _P, _P, _P, _P, _P]),
     "sp_cg_update_f64": (c_int32, [c_int64, c_double, _P, _P, _P, _P, _P, _P, _P]),
     "sp_cg_update_f32": (c_int32, [c_int64, c_double, _P, _P, _P, _P, _P, _P, _P]),
+    "sp_cg_update_ref_f64": (c_int32, [c_int64, c_double, _P, _P, _P, _P, _P]),
+    "sp_cg_update_ref_f32": (c_int32, [c_int64, c_double, _P, _P, _P, _P, _P]),
     "sp_ogs_setup_csr": (c_int32, [c_int32, _I64P, c_int32, c_int32, _I32P, _I32P, _I32P,
                                    _I32P, _I32P, _I32P]),
     "sp_ogs_setup": (c_int32, [c_int32, _I64P, c_int32, c_int32, _P, POINTER(c_void_p)]),

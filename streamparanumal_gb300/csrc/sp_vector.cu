@@ -604,8 +604,9 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
   finish_ticket(bv, sc, out, s);
 }
 
-// x += alpha p ; r -= alpha Ap ; out = sum r*r     (FP64 storage)
-template <int U>
+// FULL: x += alpha p ; r -= alpha Ap ; out = sum r*r     (FP64 storage)
+// !FULL (the reference's BS5 update): r += alpha Ap ; out = sum r*r
+template <int U, bool FULL = true>
 __global__ void __launch_bounds__(kRedThreads)
 k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double2* __restrict__ Ap,
          double2* __restrict__ x, double2* __restrict__ r, const double* __restrict__ ps,
@@ -622,22 +623,28 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + (int64_t)u * kRedThreads;
       if (i < nvec) {
-        vp[u] = __ldcs(p + i);
+        if (FULL) {
+          vp[u] = __ldcs(p + i);
+          vx[u] = __ldcs(x + i);
+        }
         va[u] = __ldcs(Ap + i);
-        vx[u] = __ldcs(x + i);
         vr[u] = __ldcs(r + i);
       }
     }
+    const double ar = FULL ? -alpha : alpha;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + (int64_t)u * kRedThreads;
       if (i < nvec) {
-        double2 nx, nr;
-        nx.x = fma(alpha, vp[u].x, vx[u].x);
-        nx.y = fma(alpha, vp[u].y, vx[u].y);
-        nr.x = fma(-alpha, va[u].x, vr[u].x);
-        nr.y = fma(-alpha, va[u].y, vr[u].y);
-        __stcs(x + i, nx);
+        double2 nr;
+        if (FULL) {
+          double2 nx;
+          nx.x = fma(alpha, vp[u].x, vx[u].x);
+          nx.y = fma(alpha, vp[u].y, vx[u].y);
+          __stcs(x + i, nx);
+        }
+        nr.x = fma(ar, va[u].x, vr[u].x);
+        nr.y = fma(ar, va[u].y, vr[u].y);
         __stcs(r + i, nr);
         acc0 = fma(nr.x, nr.x, acc0);
         acc1 = fma(nr.y, nr.y, acc1);
@@ -646,8 +653,8 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
     const int64_t t = n - 1;
-    xs[t] = fma(alpha, ps[t], xs[t]);
-    const double nr = fma(-alpha, Aps[t], rs[t]);
+    if (FULL) xs[t] = fma(alpha, ps[t], xs[t]);
+    const double nr = fma(FULL ? -alpha : alpha, Aps[t], rs[t]);
     rs[t] = nr;
     acc0 = fma(nr, nr, acc0);
   }
@@ -656,8 +663,8 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
 }
 
 // FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
-// r.r with compensated FP32 lanes and an FP64 cross-block finish.
-template <int U>
+// r.r with compensated FP32 lanes and an FP64 cross-block finish.  FULL as k_cg_f64.
+template <int U, bool FULL = true>
 __global__ void __launch_bounds__(kRedThreads)
 k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* __restrict__ Ap,
          float4* __restrict__ x, float4* __restrict__ r, const float* __restrict__ ps,
@@ -674,26 +681,32 @@ k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* 
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + (int64_t)u * kRedThreads;
       if (i < nvec) {
-        vp[u] = __ldcs(p + i);
+        if (FULL) {
+          vp[u] = __ldcs(p + i);
+          vx[u] = __ldcs(x + i);
+        }
         va[u] = __ldcs(Ap + i);
-        vx[u] = __ldcs(x + i);
         vr[u] = __ldcs(r + i);
       }
     }
+    const float ar = FULL ? -alpha : alpha;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + (int64_t)u * kRedThreads;
       if (i < nvec) {
-        float4 nx, nr;
-        nx.x = fmaf(alpha, vp[u].x, vx[u].x);
-        nx.y = fmaf(alpha, vp[u].y, vx[u].y);
-        nx.z = fmaf(alpha, vp[u].z, vx[u].z);
-        nx.w = fmaf(alpha, vp[u].w, vx[u].w);
-        nr.x = fmaf(-alpha, va[u].x, vr[u].x);
-        nr.y = fmaf(-alpha, va[u].y, vr[u].y);
-        nr.z = fmaf(-alpha, va[u].z, vr[u].z);
-        nr.w = fmaf(-alpha, va[u].w, vr[u].w);
-        __stcs(x + i, nx);
+        float4 nr;
+        if (FULL) {
+          float4 nx;
+          nx.x = fmaf(alpha, vp[u].x, vx[u].x);
+          nx.y = fmaf(alpha, vp[u].y, vx[u].y);
+          nx.z = fmaf(alpha, vp[u].z, vx[u].z);
+          nx.w = fmaf(alpha, vp[u].w, vx[u].w);
+          __stcs(x + i, nx);
+        }
+        nr.x = fmaf(ar, va[u].x, vr[u].x);
+        nr.y = fmaf(ar, va[u].y, vr[u].y);
+        nr.z = fmaf(ar, va[u].z, vr[u].z);
+        nr.w = fmaf(ar, va[u].w, vr[u].w);
         __stcs(r + i, nr);
         dot2_step(nr.x, nr.x, sum, comp);
         dot2_step(nr.y, nr.y, sum, comp);
@@ -704,8 +717,8 @@ k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* 
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     for (int64_t t = nvec * 4; t < n; ++t) {
-      xs[t] = fmaf(alpha, ps[t], xs[t]);
-      const float nr = fmaf(-alpha, Aps[t], rs[t]);
+      if (FULL) xs[t] = fmaf(alpha, ps[t], xs[t]);
+      const float nr = fmaf(FULL ? -alpha : alpha, Aps[t], rs[t]);
       rs[t] = nr;
       dot2_step(nr, nr, sum, comp);
     }
@@ -883,6 +896,30 @@ sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float*
       nvec, (float)alpha, reinterpret_cast<const float4*>(p), reinterpret_cast<const float4*>(Ap),
       reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r), p, Ap, x, r, n, scratch, rdotr);
   return check_launch("sp_cg_update_f32");
+}
+
+sp_status sp_cg_update_ref_f64(int64_t n, double alpha, const double* Ap, double* r,
+                               double* rdotr, void* scratch, sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, rdotr, {Ap, r}, "sp_cg_update_ref_f64");
+  if (st) return st;
+  constexpr int U = 2;
+  const int64_t nvec = n / 2;
+  k_cg_f64<U, false><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, alpha, nullptr, reinterpret_cast<const double2*>(Ap), nullptr,
+      reinterpret_cast<double2*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr);
+  return check_launch("sp_cg_update_ref_f64");
+}
+
+sp_status sp_cg_update_ref_f32(int64_t n, double alpha, const float* Ap, float* r,
+                               double* rdotr, void* scratch, sp_stream_t stream) {
+  sp_status st = check_red_args(n, scratch, rdotr, {Ap, r}, "sp_cg_update_ref_f32");
+  if (st) return st;
+  constexpr int U = 2;
+  const int64_t nvec = n / 4;
+  k_cg_f32<U, false><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+      nvec, (float)alpha, nullptr, reinterpret_cast<const float4*>(Ap), nullptr,
+      reinterpret_cast<float4*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr);
+  return check_launch("sp_cg_update_ref_f32");
 }
 
 // ------------------------------------------------------------------ BS0 graph form

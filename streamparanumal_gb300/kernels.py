@@ -151,3 +151,14 @@ def cg_update(alpha: float, o_p, o_Ap, o_x, o_r, o_rdotr, scratch: ReduceScratch
     fn = "sp_cg_update_f64" if o_p.dtype == torch.float64 else "sp_cg_update_f32"
     capi.call(fn, o_p.numel(), float(alpha), o_p.data_ptr(), o_Ap.data_ptr(), o_x.data_ptr(),
               o_r.data_ptr(), o_rdotr.data_ptr(), scratch.ptr, _stream(stream))
+
+
+def cg_update_ref(alpha: float, o_Ap, o_r, o_rdotr, scratch: ReduceScratch, stream=None) -> None:
+    """The reference's BS5 update in one launch: r += alpha Ap; rdotr[0] = r.r (FP64;
+    fixed-grid order, compensated FP32 lanes for float32 storage)."""
+    _chk(o_Ap, (torch.float64, torch.float32), "o_Ap")
+    _chk(o_r, (o_Ap.dtype,), "o_r")
+    _chk(o_rdotr, (torch.float64,), "o_rdotr")
+    fn = "sp_cg_update_ref_f64" if o_Ap.dtype == torch.float64 else "sp_cg_update_ref_f32"
+    capi.call(fn, o_Ap.numel(), float(alpha), o_Ap.data_ptr(), o_r.data_ptr(),
+              o_rdotr.data_ptr(), scratch.ptr, _stream(stream))

@@ -191,6 +191,26 @@ def test_cg_update_fp32_storage(cuda, orc, n):
     assert abs(host(rr)[0] - rrref) <= 1e-6 * rrref
 
 
+@pytest.mark.parametrize("n", [1, 2, 5, 1001, 65536, (1 << 21) + 3])
+@pytest.mark.parametrize("f32", [False, True])
+def test_cg_update_reference_form(cuda, orc, n, f32):
+    """r += alpha Ap (bit-exact fma / fmaf) and r.r (FP64 1e-14 of the double-double
+    sum; FP32 storage 1e-6) in one launch."""
+    r, Ap = (orc.uniform(n, 20 * s + n) for s in (1, 2))
+    if f32:
+        r, Ap = r.astype(np.float32), Ap.astype(np.float32)
+    alpha = 0.318309886
+    dr = dev(r)
+    sc = K.ReduceScratch()
+    rr = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.cg_update_ref(alpha, dev(Ap), dr, rr, sc)
+    # the oracle's full update with -alpha leaves r = fma(alpha, Ap, r)
+    a = np.float32(-alpha) if f32 else -alpha
+    _, rref, rrref = orc.cg_update(a, Ap, Ap, np.zeros_like(r), r)
+    np.testing.assert_array_equal(host(dr), rref)
+    assert abs(host(rr)[0] - rrref) <= (1e-6 if f32 else 8e-14) * rrref
+
+
 def test_bs0_and_graph(cuda):
     a = torch.zeros(1, dtype=torch.float64, device="cuda")
     b = torch.full((1,), 5.0, dtype=torch.float64, device="cuda")
