@@ -2,8 +2,9 @@
 // same output rows as the reference's BS/BS{0..5}/src/bs*Run.cpp; the kernels are
 // built by platform_t::buildKernel and run through libspgb300.
 // Added option: -fp/--precision FP32 runs the FP32-storage forms (BS1 copy, BS2
-// axpy, BS3 norm and BS4 dot with compensated FP32 lanes, BS5 as the full CG
-// update); -cg/--cg-full TRUE runs BS5 as the full CG update in FP64.
+// axpy, BS3 norm and BS4 dot with compensated FP32 lanes, BS5's r += alpha Ap and
+// r.r in one launch); -cg/--cg-full TRUE runs BS5 as the full CG update
+// x += alpha p, r -= alpha Ap, r.r (FP64 or FP32 storage).
 #include <string>
 
 #include "bs.hpp"
@@ -137,7 +138,7 @@ int nblock_for(size_t N, int blockSize) {
 // BS4 dot (bs4Run.cpp:29-99), BS5 CG update (bs5Run.cpp:29-103).
 void bsVecRun(int which, platform_t& platform, settings_t& settings) {
   const bool fp32 = settings.compareSetting("PRECISION", "FP32");
-  const bool cgFull = (which == 5) && (fp32 || settings.compareSetting("CG FULL", "TRUE"));
+  const bool cgFull = (which == 5) && settings.compareSetting("CG FULL", "TRUE");
   const size_t word = fp32 ? sizeof(float) : sizeof(dfloat);
   // entries moved per DOF by each benchmark (the reference's `sc` / word size)
   const size_t perEntry[6] = {0, 2, 3, 1, 2, cgFull ? 6 : 3};
@@ -190,9 +191,14 @@ void bsVecRun(int which, platform_t& platform, settings_t& settings) {
           checkStatus(sp_dot_f32(N, v32[0].ptr(), v32[1].ptr(), o_res.ptr(), scratch, s), "BS4");
           break;
         case 5:
-          checkStatus(sp_cg_update_f32(N, alpha, v32[0].ptr(), v32[1].ptr(), v32[2].ptr(),
-                                       v32[3].ptr(), o_res.ptr(), scratch, s),
-                      "BS5");
+          if (cgFull)
+            checkStatus(sp_cg_update_f32(N, alpha, v32[0].ptr(), v32[1].ptr(), v32[2].ptr(),
+                                         v32[3].ptr(), o_res.ptr(), scratch, s),
+                        "BS5");
+          else
+            checkStatus(sp_cg_update_ref_f32(N, alpha, v32[0].ptr(), v32[1].ptr(), o_res.ptr(),
+                                             scratch, s),
+                        "BS5");
           break;
       }
       return;
