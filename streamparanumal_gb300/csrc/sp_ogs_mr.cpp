@@ -18,6 +18,8 @@
 //     after it in ascending rank order (ogsPairwise_t, ogsPairwise.cpp:176-387).
 // Every rank runs the same sequence of collectives, also after a local error: an
 // error flag is reduced at the end, so that all ranks fail together.
+#include <parallel/algorithm>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -91,7 +93,8 @@ template <class Key>
 std::vector<int64_t> stable_order(int64_t n, Key key) {
   std::vector<int64_t> o((size_t)n);
   std::iota(o.begin(), o.end(), 0);
-  std::stable_sort(o.begin(), o.end(), [&](int64_t a, int64_t b) { return key(a) < key(b); });
+  __gnu_parallel::stable_sort(o.begin(), o.end(),
+                              [&](int64_t a, int64_t b) { return key(a) < key(b); });
   return o;
 }
 
