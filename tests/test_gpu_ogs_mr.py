@@ -181,3 +181,56 @@ def test_gpu_ranks_without_nodes_or_ids(cuda, orc):
                                                        O.Add, O.Sym, ex[c.rank]))
     for r in range(P):
         np.testing.assert_array_equal(got[r], want[r])
+
+
+def _torchcomm_rank(rank, world, port, path, q):
+    import torch.distributed as dist
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        from oracle import oracle as orc
+        orc.load()
+        torch.cuda.set_device(0)
+        case = json.loads(Path(path).read_text())
+        z = np.load(GOLDEN / case["ids_file"])
+        ids = z[f"r{rank}"].copy()
+        comm = C.TorchComm()
+        o = O.ogs_t()
+        s = torch.cuda.Stream()
+        o.Setup(ids.size, ids, comm, O.Signed, O.Pairwise, False, stream=s)
+        v = torch.from_numpy(orc.uniform(o.N, case["qseed"] + 1000 * rank)).cuda()
+        res = {}
+        for m, name in ((O.Sym, "sym"), (O.NoTrans, "notrans"), (O.Trans, "trans")):
+            w = v.clone()
+            o.GatherScatter(w, 1, O.Add, m, stream=s)
+            s.synchronize()
+            res[name] = sha(w.cpu().numpy())
+        q.put((rank, res))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gpu_torchcomm_processes_match_the_reference(cuda):
+    """Two processes on this GPU over a gloo group: the halo rows travel through
+    host memory (TorchComm), as the reference's exchange does without GPU-aware MPI;
+    every mode matches the reference's own results bit for bit."""
+    import socket
+    import torch.multiprocessing as mp
+    path = GOLDEN / "ogsmr_2r_2x2x2_p2.json"
+    case = json.loads(path.read_text())
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_torchcomm_rank, args=(r, 2, port, str(path), q))
+             for r in range(2)]
+    for p in procs:
+        p.start()
+    out = dict(q.get(timeout=300) for _ in range(2))
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    for r in range(2):
+        for name in ("sym", "notrans", "trans"):
+            assert out[r][name] == case["per_rank"][r]["sha256"]["gs_" + name], (r, name)
