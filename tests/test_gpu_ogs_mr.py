@@ -234,3 +234,23 @@ def test_gpu_torchcomm_processes_match_the_reference(cuda):
     for r in range(2):
         for name in ("sym", "notrans", "trans"):
             assert out[r][name] == case["per_rank"][r]["sha256"]["gs_" + name], (r, name)
+
+
+def test_gpu_unsigned_kind(cuda, orc):
+    P = 2
+    ids = [O.box_hex_ids(2, 2, 1, 2, 0, size=P, rank=r) for r in range(P)]
+    hs = setup_ranks(ids, unique=False, kind=O.Unsigned)
+    views = [M.FromOgs(o) for o, _ in hs]
+    rng = np.random.default_rng(9)
+    vals = [rng.integers(-7, 8, o.N).astype(np.int64) for o, _ in hs]
+    for m in (O.Sym, O.NoTrans, O.Trans):
+        def gs(o, s, r):
+            v = torch.from_numpy(vals[r]).cuda()
+            o.GatherScatter(v, 1, O.Add, m, stream=s)
+            return v.cpu().numpy()
+        got = on_ranks(hs, gs)
+        ex = M.thread_exchanges(P)
+        want = C.run_threads(P, lambda c: M.gather_scatter(views[c.rank], orc, vals[c.rank], 1,
+                                                           O.Add, m, ex[c.rank]))
+        for r in range(P):
+            np.testing.assert_array_equal(got[r], want[r], err_msg=f"mode {m} rank {r}")
