@@ -47,7 +47,8 @@ class OgsInfo(ctypes.Structure):
     _fields_ = [("N", c_int32), ("NrowsT", c_int32), ("NrowsN", c_int32), ("nnzT", c_int32),
                 ("nnzN", c_int32), ("NrowBlocksT", c_int32), ("NrowBlocksN", c_int32),
                 ("maxRowSize", c_int32), ("NgatherGlobal", c_int64), ("NchunksT", c_int32),
-                ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32)]
+                ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32),
+                ("NchunksGS", c_int32), ("gsRowOrder", c_int32)]
 
 
 class MrInfo(ctypes.Structure):

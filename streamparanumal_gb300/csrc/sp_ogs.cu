@@ -1459,6 +1459,8 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->NchunksN = p->nchunksN;
   info->chunkOrder = p->chunk_order;
   info->rowOrder = p->row_order;
+  info->NchunksGS = p->nchunksGS;
+  info->gsRowOrder = p->gs_grouped;
   return SP_SUCCESS;
 }
 

@@ -324,6 +324,10 @@ def test_ball_chains_and_gather_scatter_walks(cuda, orc, knobs, box):
         nx, ny, nz, p, seed = box
         ids = O.box_hex_ids(nx, ny, nz, p, seed)
         h, ref = make(orc, ids)
+        gs_walk = knobs.get("ogs.gs_order", -1) >= 0
+        assert (h.info.NchunksGS > 0) == gs_walk
+        if gs_walk:
+            assert h.info.gsRowOrder == capi.tune_get("ogs.rows")
         q = orc.uniform(ids.size, 61)
         for op in (O.Add, O.Max):
             dq = torch.from_numpy(q).cuda()
