@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 #include <vector>
 
 #include "sp_ogs_plan.h"
@@ -755,6 +756,40 @@ k_ogsc_scatter(int32_t N, const int32_t* __restrict__ rowOfCol, const T* __restr
   }
 }
 
+// The same with 16-byte accesses: each thread takes 16 / sizeof(T) consecutive
+// columns (one int4 or int2 of row ids, one 16-byte store), for 16-byte-aligned v
+// and N a multiple of that width.  A column in no row keeps its value: the old
+// vector is read only when the group holds such a column.
+template <typename T> struct Vec16Of;
+template <> struct Vec16Of<float> { using type = float4; };
+template <> struct Vec16Of<double> { using type = double2; };
+template <> struct Vec16Of<int32_t> { using type = int4; };
+template <> struct Vec16Of<long long> { using type = longlong2; };
+
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogsc_scatter_vec(int64_t nvec, const int32_t* __restrict__ rowOfCol, const T* __restrict__ gv,
+                   T* __restrict__ v) {
+  constexpr int V = 16 / sizeof(T);
+  using IV = typename std::conditional<V == 4, int4, int2>::type;
+  using TV = typename Vec16Of<T>::type;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nvec;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const IV rv = __ldg(reinterpret_cast<const IV*>(rowOfCol) + i);
+    const int32_t* r = reinterpret_cast<const int32_t*>(&rv);
+    bool any_free = false;
+#pragma unroll
+    for (int k = 0; k < V; ++k) any_free |= r[k] < 0;
+    TV out;
+    T* o = reinterpret_cast<T*>(&out);
+    if (any_free) out = reinterpret_cast<const TV*>(v)[i];
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      if (r[k] >= 0) o[k] = gv[r[k]];
+    reinterpret_cast<TV*>(v)[i] = out;
+  }
+}
+
 // Persistent column-order scatter (kernel 4 for scatters on T chunks): as kernel 3,
 // with each warp walking chunks c, c+W, ... and bulk-prefetching the next chunk's
 // three contiguous ranges (column ids, row offsets, gv slice) into L2 before
@@ -951,8 +986,17 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
   const bool useN = (trans == SP_TRANS);
   const int kv = variant(kTuneOgsKernelScatter, K, useN ? p->nchunksN : p->nchunksT);
   if (kv == 5 && !useN && p->d_rowOfColT) {
-    const int64_t want = ((int64_t)p->N + kOgsThreads - 1) / kOgsThreads;
+    constexpr int V = 16 / sizeof(T);
     const int64_t cap = (int64_t)sm_count() * 64;
+    if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 && p->N % V == 0) {
+      const int64_t nvec = p->N / V;
+      const int64_t want = (nvec + kOgsThreads - 1) / kOgsThreads;
+      k_ogsc_scatter_vec<T>
+          <<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), kOgsThreads, 0, s>>>(
+              nvec, p->d_rowOfColT, gv, v);
+      return;
+    }
+    const int64_t want = ((int64_t)p->N + kOgsThreads - 1) / kOgsThreads;
     k_ogsc_scatter<T><<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), kOgsThreads, 0, s>>>(
         p->N, p->d_rowOfColT, gv, v);
     return;
