@@ -757,9 +757,10 @@ k_ogsc_scatter(int32_t N, const int32_t* __restrict__ rowOfCol, const T* __restr
 }
 
 // The same with 16-byte accesses: each thread takes 16 / sizeof(T) consecutive
-// columns (one int4 or int2 of row ids, one 16-byte store), for 16-byte-aligned v
-// and N a multiple of that width.  A column in no row keeps its value: the old
-// vector is read only when the group holds such a column.
+// columns (one int4 or int2 of row ids, one 16-byte store), for 16-byte-aligned v;
+// the last N mod that width columns are copied one per thread by the first block.
+// A column in no row keeps its value: the old vector is read only when the group
+// holds such a column.
 template <typename T> struct Vec16Of;
 template <> struct Vec16Of<float> { using type = float4; };
 template <> struct Vec16Of<double> { using type = double2; };
@@ -768,11 +769,17 @@ template <> struct Vec16Of<long long> { using type = longlong2; };
 
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads)
-k_ogsc_scatter_vec(int64_t nvec, const int32_t* __restrict__ rowOfCol, const T* __restrict__ gv,
+k_ogsc_scatter_vec(int64_t N, const int32_t* __restrict__ rowOfCol, const T* __restrict__ gv,
                    T* __restrict__ v) {
   constexpr int V = 16 / sizeof(T);
   using IV = typename std::conditional<V == 4, int4, int2>::type;
   using TV = typename Vec16Of<T>::type;
+  const int64_t nvec = N / V;
+  if (blockIdx.x == 0 && threadIdx.x < N - nvec * V) {
+    const int64_t i = nvec * V + threadIdx.x;
+    const int32_t r = __ldg(rowOfCol + i);
+    if (r >= 0) v[i] = gv[r];
+  }
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nvec;
        i += (int64_t)gridDim.x * blockDim.x) {
     const IV rv = __ldg(reinterpret_cast<const IV*>(rowOfCol) + i);
@@ -988,12 +995,11 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
   if (kv == 5 && !useN && p->d_rowOfColT) {
     constexpr int V = 16 / sizeof(T);
     const int64_t cap = (int64_t)sm_count() * 64;
-    if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 && p->N % V == 0) {
-      const int64_t nvec = p->N / V;
-      const int64_t want = (nvec + kOgsThreads - 1) / kOgsThreads;
+    if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+      const int64_t want = (p->N / V + kOgsThreads - 1) / kOgsThreads;
       k_ogsc_scatter_vec<T>
           <<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), kOgsThreads, 0, s>>>(
-              nvec, p->d_rowOfColT, gv, v);
+              (int64_t)p->N, p->d_rowOfColT, gv, v);
       return;
     }
     const int64_t want = ((int64_t)p->N + kOgsThreads - 1) / kOgsThreads;

@@ -377,3 +377,28 @@ def test_page_sizes_of_breadth_first_order(cuda, orc, shift, order):
     finally:
         for k, v in old.items():
             capi.tune_set(k, v)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 81, 405, 1001, 4099])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset):
+    """The column-major scatter with 16-byte accesses (kernel 5) for every length
+    modulo the vector width, with columns in no row (id 0) keeping their values and
+    the vector shifted off its 16-byte alignment (the one-column form then runs)."""
+    old = capi.tune_get("ogs.kernel.scatter")
+    try:
+        capi.tune_set("ogs.kernel.scatter", 5)
+        rng = np.random.default_rng(n * 7 + offset)
+        ids = rng.integers(-max(2, n // 3), max(2, n // 3) + 1, n).astype(np.int64)
+        ids[0] = ids[0] or 1
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        g = values(orc, rs.size - 1, dtype, 17)
+        base = values(orc, n, dtype, 19)
+        store = torch.from_numpy(np.concatenate([np.zeros(offset, dtype), base])).cuda()
+        dq = store[offset:]
+        h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)
+        np.testing.assert_array_equal(host(dq), orc.scatter(rs, ci, g, base))
+    finally:
+        capi.tune_set("ogs.kernel.scatter", old)
