@@ -81,7 +81,10 @@ void        sp_launch_count_reset(void);
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
  *    the column-order scatter, 4 column-order pipelined gathers or the persistent
  *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch or
- *    the column-major scatter (one thread per local column); defaults 2, 2, 5.
+ *    the column-major scatter (one thread per local column); defaults 2, 2, 5;
+ *  "ogs.scatter_pages" (1 = the column-major scatter takes the pages of local
+ *    columns in the main walk's order when the plan has one (chunk orders 1 and 2),
+ *    0 = in memory order; default 1).
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);

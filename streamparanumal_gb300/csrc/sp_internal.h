@@ -53,6 +53,7 @@ enum TuneKey : int {
   kTuneOgsGsOrder,          // ogs plan: -1 gather+scatter on the main walk, else its own walk's order
   kTuneOgsGsPageShift,      // ogs plan: page size of the gather+scatter walk
   kTuneOgsGsBallShift,      // ogs plan: ball size of the gather+scatter walk
+  kTuneOgsScatterPages,     // ogs column-major scatter: 1 = pages in the main walk's order
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -797,6 +797,49 @@ k_ogsc_scatter_vec(int64_t N, const int32_t* __restrict__ rowOfCol, const T* __r
   }
 }
 
+// The 16-byte column-major scatter with the pages of local columns taken in the
+// main walk's visit order instead of memory order: group g (V columns) lies in the
+// (g*V >> shift)-th visited page.  On a mesh whose elements sit at random places,
+// the rows an element shares with its neighbours were numbered inside those
+// neighbours, so in memory order each such row is fetched once per element that
+// holds it, from far apart in time; in walk order the neighbours run close
+// together and the second fetch usually hits L2.  Stores stay contiguous within a
+// page.  Requires 16-byte-aligned v and 2^shift >= V.
+template <typename T>
+__global__ void __launch_bounds__(kOgsThreads)
+k_ogsc_scatter_pages(int64_t ngroups, const int32_t* __restrict__ pages, int shift, int64_t N,
+                     const int32_t* __restrict__ rowOfCol, const T* __restrict__ gv,
+                     T* __restrict__ v) {
+  constexpr int V = 16 / sizeof(T);
+  using IV = typename std::conditional<V == 4, int4, int2>::type;
+  using TV = typename Vec16Of<T>::type;
+  const int64_t mask = ((int64_t)1 << shift) - 1;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ngroups;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = g * V;
+    const int64_t c = ((int64_t)__ldg(pages + (x >> shift)) << shift) + (x & mask);
+    if (c + V <= N) {
+      const IV rv = __ldg(reinterpret_cast<const IV*>(rowOfCol + c));
+      const int32_t* r = reinterpret_cast<const int32_t*>(&rv);
+      bool any_free = false;
+#pragma unroll
+      for (int k = 0; k < V; ++k) any_free |= r[k] < 0;
+      TV out;
+      T* o = reinterpret_cast<T*>(&out);
+      if (any_free) out = *reinterpret_cast<const TV*>(v + c);
+#pragma unroll
+      for (int k = 0; k < V; ++k)
+        if (r[k] >= 0) o[k] = gv[r[k]];
+      *reinterpret_cast<TV*>(v + c) = out;
+    } else {
+      for (int64_t i = c; i < N; ++i) {
+        const int32_t r = __ldg(rowOfCol + i);
+        if (r >= 0) v[i] = gv[r];
+      }
+    }
+  }
+}
+
 // Persistent column-order scatter (kernel 4 for scatters on T chunks): as kernel 3,
 // with each warp walking chunks c, c+W, ... and bulk-prefetching the next chunk's
 // three contiguous ranges (column ids, row offsets, gv slice) into L2 before
@@ -995,6 +1038,15 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
   if (kv == 5 && !useN && p->d_rowOfColT) {
     constexpr int V = 16 / sizeof(T);
     const int64_t cap = (int64_t)sm_count() * 64;
+    if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 && p->d_pagesT &&
+        tune(kTuneOgsScatterPages) == 1 && ((int64_t)1 << p->pages_shift) >= V) {
+      const int64_t ngroups = ((int64_t)p->npagesT << p->pages_shift) / V;
+      const int64_t want = (ngroups + kOgsThreads - 1) / kOgsThreads;
+      k_ogsc_scatter_pages<T>
+          <<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), kOgsThreads, 0, s>>>(
+              ngroups, p->d_pagesT, p->pages_shift, (int64_t)p->N, p->d_rowOfColT, gv, v);
+      return;
+    }
     if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
       const int64_t want = (p->N / V + kOgsThreads - 1) / kOgsThreads;
       k_ogsc_scatter_vec<T>
@@ -1156,6 +1208,9 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->d_walkRsT = p->d_walkCiT = p->d_permT = nullptr;
   if (p->d_rowOfColT) cudaFree(p->d_rowOfColT);
   p->d_rowOfColT = nullptr;
+  if (p->d_pagesT) cudaFree(p->d_pagesT);
+  p->d_pagesT = nullptr;
+  p->npagesT = 0;
   if (p->d_chunksGS) cudaFree(p->d_chunksGS);
   if (p->d_rsGS) cudaFree(p->d_rsGS);
   if (p->d_ciGS) cudaFree(p->d_ciGS);
@@ -1338,7 +1393,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
   const int page_shift = (int)tune(kTuneOgsPageShift);
   const int ball_shift = (int)tune(kTuneOgsBallShift);
   const bool renumber = p->chunk_order == 2;
-  std::vector<int32_t> walkRs, walkCi, perm;
+  std::vector<int32_t> walkRs, walkCi, perm, pages;
   const int32_t* wrs = p->rowStartsT.data();
   const int32_t* wci = p->colIdsT.data();
   std::vector<int32_t> chunksT, chunksN;
@@ -1350,7 +1405,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       if (p->rowStartsT[r + 1] - p->rowStartsT[r] > kWarpChunkNnz) tooBig = 1;
     fits = !tooBig;
     if (fits) {
-      bfs_row_sequence(p->NrowsT, wrs, wci, p->N, page_shift, ball_shift, perm);
+      bfs_row_sequence(p->NrowsT, wrs, wci, p->N, page_shift, ball_shift, perm, &pages);
       walkRs.assign((size_t)p->NrowsT + 1, 0);
       for (int32_t k = 0; k < p->NrowsT; ++k)
         walkRs[k + 1] = walkRs[k] + (p->rowStartsT[perm[k] + 1] - p->rowStartsT[perm[k]]);
@@ -1365,7 +1420,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     }
   } else {
     fits = build_chunks(p->NrowsT, wrs, wci, p->N, p->chunk_order, chunksT, page_shift,
-                        ball_shift);
+                        ball_shift, p->chunk_order == 1 ? &pages : nullptr);
   }
   if (fits && build_chunks(p->NrowsN, p->rowStartsN.data(), p->colIdsN.data(), p->N, 0, chunksN,
                            page_shift, 0)) {
@@ -1421,6 +1476,11 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     for (int32_t r = 0; r < p->NrowsT; ++r)
       for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) rowOfCol[p->colIdsT[i]] = r;
     if ((st = upload(rowOfCol, &p->d_rowOfColT, s))) return st;
+    if (!pages.empty()) {
+      p->npagesT = (int32_t)pages.size();
+      p->pages_shift = page_shift;
+      if ((st = upload(pages, &p->d_pagesT, s))) return st;
+    }
     if ((st = build_gs_walk(p, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   } else {

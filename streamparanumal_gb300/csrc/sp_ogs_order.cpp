@@ -259,7 +259,8 @@ static void page_order(int32_t nrows, const int32_t* rs, const int32_t* ci, int3
 }
 
 bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols, int order,
-                  std::vector<int32_t>& chunks, int page_shift, int ball_shift) {
+                  std::vector<int32_t>& chunks, int page_shift, int ball_shift,
+                  std::vector<int32_t>* pages) {
   chunks.clear();
   int32_t tooBig = 0;
 #pragma omp parallel for schedule(static) reduction(max : tooBig)
@@ -273,6 +274,7 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
   }
   PageOrder po;
   page_order(nrows, rs, ci, ncols, page_shift, ball_shift, po);
+  if (pages) *pages = po.queue;
   const int32_t npages = po.npages, nonEmpty = po.nonEmpty;
   const std::vector<int32_t>& rowPage = po.rowPage;
   const std::vector<int32_t>& pageRows = po.pageRows;
@@ -315,11 +317,13 @@ bool build_chunks(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t n
 }
 
 void bfs_row_sequence(int32_t nrows, const int32_t* rs, const int32_t* ci, int32_t ncols,
-                      int page_shift, int ball_shift, std::vector<int32_t>& seq) {
+                      int page_shift, int ball_shift, std::vector<int32_t>& seq,
+                      std::vector<int32_t>* pages) {
   seq.clear();
   if (nrows == 0) return;
   PageOrder po;
   page_order(nrows, rs, ci, ncols, page_shift, ball_shift, po);
+  if (pages) *pages = po.queue;
   seq.resize(nrows);
   std::vector<int64_t> at(po.npages + 1, 0);
   for (int32_t k = 0; k < po.npages; ++k) {

@@ -46,14 +46,17 @@ bool partition_rows(int32_t nrows, const int32_t* rowStarts, std::vector<int32_t
 // order they are scheduled: 0 = row order, 1 = breadth-first over pages of
 // 2^page_shift local entries (ball_shift > 0: a chain of breadth-first balls of
 // 2^ball_shift entries).  Returns false when a row holds more than kWarpChunkNnz
-// entries.
+// entries.  For order 1, `pages` (if given) receives the pages in visit order.
 bool build_chunks(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds, int32_t ncols,
-                  int order, std::vector<int32_t>& chunks, int page_shift, int ball_shift);
+                  int order, std::vector<int32_t>& chunks, int page_shift, int ball_shift,
+                  std::vector<int32_t>* pages = nullptr);
 
 // All rows in breadth-first page order: each page's rows (ascending) as the pages
-// are visited, then rows without members.  seq[k] = the k-th row of the walk.
+// are visited, then rows without members.  seq[k] = the k-th row of the walk;
+// `pages` (if given) receives the pages in visit order.
 void bfs_row_sequence(int32_t nrows, const int32_t* rowStarts, const int32_t* colIds,
-                      int32_t ncols, int page_shift, int ball_shift, std::vector<int32_t>& seq);
+                      int32_t ncols, int page_shift, int ball_shift, std::vector<int32_t>& seq,
+                      std::vector<int32_t>* pages = nullptr);
 
 // Rows of every chunk regrouped by size.  `quads` holds the chunk descriptors
 // (r0, r1, g0, g1).  Inside chunk [r0, r1) the rows are reordered by member count,
@@ -144,6 +147,10 @@ struct sp_ogs_plan {
   // the row of T holding each local column (-1: in no row), for the column-major
   // scatter; built with the warp chunks
   int32_t* d_rowOfColT = nullptr;    // N
+  // pages of 2^pages_shift local columns in the main walk's visit order (chunk
+  // orders 1 and 2), for the column-major scatter
+  int32_t* d_pagesT = nullptr;
+  int32_t npagesT = 0, pages_shift = 0;
   // optional second walk of T for the in-place gather+scatter (knob ogs.gs_order):
   // its own chunk order, page and ball sizes, rows grouped by size or the walk CSR
   int32_t* d_chunksGS = nullptr;

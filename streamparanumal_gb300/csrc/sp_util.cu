@@ -44,6 +44,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.gs_order", -1, 2, {-1}},
     {"ogs.gs_page_shift", 3, 16, {8}},
     {"ogs.gs_ball_shift", 0, 26, {18}},
+    {"ogs.scatter_pages", 0, 1, {1}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -104,3 +104,34 @@ def test_unique_with_unsigned_kind_is_invalid(lib):
                      capi.i32p(z), capi.i32p(z))
     assert st == capi.SP_ERR_INVALID_ARG
     assert capi.last_error() == "Invalid ogs setup requested"
+
+
+KNOB_RANGES = {  # key: (lowest, highest, default), as include/sp_capi.h documents them
+    "reduce.prefetch_chunks": (-1, 64, -1), "reduce.rolling": (0, 1, 1),
+    "ogs.block_nnz": (256, 2048, 2048), "ogs.order": (0, 2, 1), "ogs.page_shift": (3, 16, 9),
+    "ogs.rows": (0, 1, 1), "ogs.ball_shift": (0, 26, 0), "ogs.gs_order": (-1, 2, -1),
+    "ogs.gs_page_shift": (3, 16, 8), "ogs.gs_ball_shift": (0, 26, 18),
+    "ogs.kernel": (0, 5, 2), "ogs.kernel.gather": (0, 5, 2), "ogs.kernel.scatter": (0, 5, 5),
+    "ogs.scatter_pages": (0, 1, 1)}
+
+
+@pytest.mark.parametrize("key", sorted(KNOB_RANGES))
+def test_tuning_knobs_ranges_and_defaults(lib, key):
+    lo, hi, default = KNOB_RANGES[key]
+    start = capi.tune_get(key)
+    try:
+        for bad in (lo - 1, hi + 1):
+            assert capi.status("sp_tune_set", key.encode(), bad) == capi.SP_ERR_INVALID_ARG
+        for good in (lo, hi):
+            capi.tune_set(key, good)
+            assert capi.tune_get(key) == good
+    finally:
+        capi.tune_set(key, start)
+    out = subprocess.run(["python", "-c", "from streamparanumal_gb300 import capi; "
+                          f"print(capi.tune_get('{key}'))"], capture_output=True, text=True,
+                         check=True).stdout
+    assert int(out) == default, "a fresh process starts from the documented default"
+
+
+def test_unknown_knob_is_rejected(lib):
+    assert capi.status("sp_tune_set", b"ogs.no_such_knob", 0) == capi.SP_ERR_INVALID_ARG

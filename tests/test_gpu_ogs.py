@@ -382,13 +382,18 @@ def test_page_sizes_of_breadth_first_order(cuda, orc, shift, order):
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 81, 405, 1001, 4099])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64])
 @pytest.mark.parametrize("offset", [0, 1])
-def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset):
+@pytest.mark.parametrize("walk", [(0, 9, 1), (1, 3, 0), (1, 3, 1), (2, 4, 1), (1, 9, 1)])
+def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset, walk):
     """The column-major scatter with 16-byte accesses (kernel 5) for every length
-    modulo the vector width, with columns in no row (id 0) keeping their values and
-    the vector shifted off its 16-byte alignment (the one-column form then runs)."""
-    old = capi.tune_get("ogs.kernel.scatter")
+    modulo the vector width, in memory order and with its pages in the walk's order
+    (chunk order, page shift, ogs.scatter_pages), with columns in no row (id 0)
+    keeping their values and the vector shifted off its 16-byte alignment (the
+    one-column form then runs)."""
+    keys = ("ogs.kernel.scatter", "ogs.order", "ogs.page_shift", "ogs.scatter_pages")
+    old = {k: capi.tune_get(k) for k in keys}
     try:
-        capi.tune_set("ogs.kernel.scatter", 5)
+        for k, x in zip(keys, (5,) + walk):
+            capi.tune_set(k, x)
         rng = np.random.default_rng(n * 7 + offset)
         ids = rng.integers(-max(2, n // 3), max(2, n // 3) + 1, n).astype(np.int64)
         ids[0] = ids[0] or 1
@@ -401,4 +406,5 @@ def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset):
         h.Scatter(dq, torch.from_numpy(g).cuda(), 1, O.NoTrans)
         np.testing.assert_array_equal(host(dq), orc.scatter(rs, ci, g, base))
     finally:
-        capi.tune_set("ogs.kernel.scatter", old)
+        for k, x in old.items():
+            capi.tune_set(k, x)
