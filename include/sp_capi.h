@@ -83,8 +83,8 @@ void        sp_launch_count_reset(void);
  *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch or
  *    the column-major scatter (one thread per local column); defaults 2, 2, 5;
  *  "ogs.scatter_pages" (1 = the column-major scatter takes the pages of local
- *    columns in the main walk's order when the plan has one (chunk orders 1 and 2),
- *    0 = in memory order; default 1).
+ *    columns in the main walk's order when the plan has one (chunk orders 1 and 2)
+ *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1).
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);

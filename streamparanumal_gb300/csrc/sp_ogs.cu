@@ -804,7 +804,8 @@ k_ogsc_scatter_vec(int64_t N, const int32_t* __restrict__ rowOfCol, const T* __r
 // neighbours, so in memory order each such row is fetched once per element that
 // holds it, from far apart in time; in walk order the neighbours run close
 // together and the second fetch usually hits L2.  Stores stay contiguous within a
-// page.  Requires 16-byte-aligned v and 2^shift >= V.
+// page.  Requires 16-byte-aligned v and 2^shift >= V (pages of at least 1 KiB are
+// used).
 template <typename T>
 __global__ void __launch_bounds__(kOgsThreads)
 k_ogsc_scatter_pages(int64_t ngroups, const int32_t* __restrict__ pages, int shift, int64_t N,
@@ -1038,8 +1039,10 @@ static void launch_scatter(const sp_ogs_plan* p, sp_transpose trans, int K, T* v
   if (kv == 5 && !useN && p->d_rowOfColT) {
     constexpr int V = 16 / sizeof(T);
     const int64_t cap = (int64_t)sm_count() * 64;
+    // walk-ordered pages pay when a page's stores are long runs: pages of 8 FP64
+    // columns (64 bytes) at random places halve the store rate
     if (K == 1 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 && p->d_pagesT &&
-        tune(kTuneOgsScatterPages) == 1 && ((int64_t)1 << p->pages_shift) >= V) {
+        tune(kTuneOgsScatterPages) == 1 && ((int64_t)sizeof(T) << p->pages_shift) >= 1024) {
       const int64_t ngroups = ((int64_t)p->npagesT << p->pages_shift) / V;
       const int64_t want = (ngroups + kOgsThreads - 1) / kOgsThreads;
       k_ogsc_scatter_pages<T>

@@ -382,7 +382,7 @@ def test_page_sizes_of_breadth_first_order(cuda, orc, shift, order):
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 81, 405, 1001, 4099])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64])
 @pytest.mark.parametrize("offset", [0, 1])
-@pytest.mark.parametrize("walk", [(0, 9, 1), (1, 3, 0), (1, 3, 1), (2, 4, 1), (1, 9, 1)])
+@pytest.mark.parametrize("walk", [(0, 9, 1), (1, 8, 0), (1, 8, 1), (2, 8, 1), (1, 9, 1), (1, 3, 1)])
 def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset, walk):
     """The column-major scatter with 16-byte accesses (kernel 5) for every length
     modulo the vector width, in memory order and with its pages in the walk's order
