@@ -82,9 +82,9 @@ KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift
          "gs_order": "ogs.gs_order", "gs_page_shift": "ogs.gs_page_shift",
          "gs_ball_shift": "ogs.gs_ball_shift",
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
-         "kernel_scatter": "ogs.kernel.scatter"}
-# plan-time knobs a table entry may leave out: the library defaults
-PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1}
+         "kernel_scatter": "ogs.kernel.scatter", "scatter_pages": "ogs.scatter_pages"}
+# knobs a table entry may leave out: the library defaults
+PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1, "scatter_pages": 1}
 GS_WALK_KERNELS = (1, 2, 3, 5)
 
 
@@ -97,13 +97,15 @@ def _set(cfg: dict) -> None:
 def _kernels(pc: dict, op: str) -> list[int]:
     """Kernel variants timed under one plan configuration: block kernels ignore the
     chunk order and row grouping, so they run once per block size; the column-order
-    scatters ignore the row grouping, so they run under grouped plans only."""
+    scatters ignore the row grouping, so they run under grouped plans only; the
+    column-major scatter runs in memory order under the plain plan and over the
+    walk's pages under the grouped breadth-first ones."""
     plain = pc["order"] == 0 and pc["rows"] == 0
     ks = [0] if plain else []
     if pc["block_nnz"] == 2048:
         if op == "BS7":
-            # the column-major scatter (5) ignores chunks: timed once, with the plain plan
-            ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else []) + ([5] if plain else [])
+            walked = pc["order"] >= 1 and pc["rows"] == 1
+            ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else []) + ([5] if plain or walked else [])
         else:
             ks += [1, 2, 3, 4, 5]
     return ks
@@ -139,7 +141,7 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                    "BS8": lambda: h.GatherScatter(q, 1, O.Add, O.Sym)}
             for op, key in OPS:
                 for k in _kernels(pc, op):
-                    _set({key: k})
+                    _set({key: k, "scatter_pages": 1})
                     timings.append((pc["order"], pc["rows"], pc["page_shift"], pc["ball_shift"],
                                     pc["block_nnz"], k, op, _time(ops[op], reps, stream)))
             h.Free()
@@ -152,12 +154,17 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
             choice = {"order": order, "rows": rows, "page_shift": shift, "ball_shift": ball}
             main, gs_ms = 0.0, None
             for op, key in OPS:
-                # block kernels and the column-major scatter do not depend on the chunk
-                # layout, so they compete under every plan configuration
+                # block kernels and the memory-order column-major scatter (timed under
+                # the plain plan) do not depend on the chunk layout, so they compete
+                # under every plan configuration
                 cands = [t for t in timings if t[6] == op and (
-                    t[:4] == layout or t[5] == 0 or (op == "BS7" and t[5] == 5))]
-                *_, bnnz, k, _, ms = min(cands, key=lambda t: t[7])
+                    t[:4] == layout or t[5] == 0 or
+                    (op == "BS7" and t[5] == 5 and t[0] == 0 and t[1] == 0))]
+                win = min(cands, key=lambda t: t[7])
+                *_, bnnz, k, _, ms = win
                 choice[key] = k
+                if op == "BS7" and k == 5:
+                    choice["scatter_pages"] = int(win[:4] == layout and order >= 1)
                 if k == 0 and (op != "BS8" or "block_nnz" not in choice):
                     choice["block_nnz"] = bnnz
                 if op == "BS8":

@@ -36,7 +36,8 @@ def test_kernel_candidates():
     plain_rows = {"order": 0, "rows": 0, "block_nnz": 2048, "page_shift": 9}
     small_blocks = {"order": 0, "rows": 0, "block_nnz": 1024, "page_shift": 9}
     assert autotune._kernels(grouped, "BS6") == [1, 2, 3, 4, 5]
-    assert autotune._kernels(grouped, "BS7") == [1, 2, 3, 4]
+    assert autotune._kernels(grouped, "BS7") == [1, 2, 3, 4, 5]
+    assert autotune._kernels(dict(grouped, rows=0), "BS7") == [1, 2]
     assert autotune._kernels(plain_rows, "BS8") == [0, 1, 2, 3, 4, 5]
     assert autotune._kernels(plain_rows, "BS7") == [0, 1, 2, 5]
     assert autotune._kernels(small_blocks, "BS6") == [0]
