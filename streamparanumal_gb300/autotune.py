@@ -111,6 +111,41 @@ def _kernels(pc: dict, op: str) -> list[int]:
     return ks
 
 
+def choose(timings: list[tuple]) -> tuple[dict, float, float]:
+    """The winner of the timed candidates (order, rows, page_shift, ball_shift,
+    block_nnz, kernel, op, ms): per chunk layout, the fastest kernel of each
+    operation; the layout with the least BS6 + BS7 time wins (BS8 breaks ties, since
+    the gather+scatter may get a walk of its own).  Returns (knobs, BS6 + BS7 ms,
+    BS8 ms)."""
+    best_key, best, best_gs_ms = None, None, None
+    for layout in sorted({t[:4] for t in timings}):
+        order, rows, shift, ball = layout
+        choice = {"order": order, "rows": rows, "page_shift": shift, "ball_shift": ball}
+        main, gs_ms = 0.0, None
+        for op, key in OPS:
+            # block kernels and the memory-order column-major scatter (timed under
+            # the plain plan) do not depend on the chunk layout, so they compete
+            # under every plan configuration
+            cands = [t for t in timings if t[6] == op and (
+                t[:4] == layout or t[5] == 0 or
+                (op == "BS7" and t[5] == 5 and t[0] == 0 and t[1] == 0))]
+            win = min(cands, key=lambda t: t[7])
+            *_, bnnz, k, _, ms = win
+            choice[key] = k
+            if op == "BS7" and k == 5:
+                choice["scatter_pages"] = int(win[:4] == layout and order >= 1)
+            if k == 0 and (op != "BS8" or "block_nnz" not in choice):
+                choice["block_nnz"] = bnnz
+            if op == "BS8":
+                gs_ms = ms
+            else:
+                main += ms
+        if best_key is None or (main, gs_ms) < best_key:
+            best_key, best, best_gs_ms = (main, gs_ms), choice, gs_ms
+    best.setdefault("block_nnz", 2048)
+    return best, best_key[0], best_gs_ms
+
+
 def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
              ids=None) -> dict:
     """Times every variant of BS6 / BS7 / BS8 on an E^3 box of degree p (ids: numpy
@@ -148,33 +183,8 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
             del gq
         # the main walk serves the gathers and scatters; the gather+scatter may get
         # a walk of its own below, so it decides the main walk only on a tie
-        best_key, best, best_gs_ms = None, None, None
-        for layout in sorted({t[:4] for t in timings}):
-            order, rows, shift, ball = layout
-            choice = {"order": order, "rows": rows, "page_shift": shift, "ball_shift": ball}
-            main, gs_ms = 0.0, None
-            for op, key in OPS:
-                # block kernels and the memory-order column-major scatter (timed under
-                # the plain plan) do not depend on the chunk layout, so they compete
-                # under every plan configuration
-                cands = [t for t in timings if t[6] == op and (
-                    t[:4] == layout or t[5] == 0 or
-                    (op == "BS7" and t[5] == 5 and t[0] == 0 and t[1] == 0))]
-                win = min(cands, key=lambda t: t[7])
-                *_, bnnz, k, _, ms = win
-                choice[key] = k
-                if op == "BS7" and k == 5:
-                    choice["scatter_pages"] = int(win[:4] == layout and order >= 1)
-                if k == 0 and (op != "BS8" or "block_nnz" not in choice):
-                    choice["block_nnz"] = bnnz
-                if op == "BS8":
-                    gs_ms = ms
-                else:
-                    main += ms
-            if best_key is None or (main, gs_ms) < best_key:
-                best_key, best, best_gs_ms = (main, gs_ms), choice, gs_ms
-        best.setdefault("block_nnz", 2048)
-        best_total = best_key[0] + best_gs_ms
+        best, main_ms, best_gs_ms = choose(timings)
+        best_total = main_ms + best_gs_ms
         # a walk of its own for the gather+scatter, on the chosen plan
         if best["order"] != 0 or best["rows"] != 0 or best.get("kernel_gs", 0) != 0:
             for w in gs_walks(p):

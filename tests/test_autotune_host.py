@@ -72,3 +72,46 @@ def test_text_form_matches_the_table():
     line = next(ln for ln in txt.splitlines() if ln.split()[0] == "p7_perm")
     fields = dict(f.split("=") for f in line.split()[1:])
     assert {autotune.KNOBS[k]: str(v) for k, v in table["p7_perm"].items()} == fields
+
+
+def _timings(ms: dict) -> list[tuple]:
+    """Synthetic timings: every candidate of plan_configs(7) at 1 ms unless listed in
+    ms ((order, rows, page_shift, ball_shift, block_nnz, kernel, op) -> ms)."""
+    out = []
+    for pc in autotune.plan_configs(7):
+        for op, _ in autotune.OPS:
+            for k in autotune._kernels(pc, op):
+                key = (pc["order"], pc["rows"], pc["page_shift"], pc["ball_shift"],
+                       pc["block_nnz"], k, op)
+                out.append(key + (ms.get(key, 1.0),))
+    return out
+
+
+def test_choose_walk_ordered_scatter_stays_with_its_layout():
+    walk = (1, 1, 9, 19, 2048)
+    best, main, gs = autotune.choose(_timings({
+        walk + (2, "BS6"): 0.5, walk + (5, "BS7"): 0.4, walk + (2, "BS8"): 0.6,
+        (0, 0, 9, 0, 2048, 5, "BS7"): 0.45}))
+    assert (best["order"], best["rows"], best["page_shift"], best["ball_shift"]) == walk[:4]
+    assert best["kernel_gather"] == 2 and best["kernel_scatter"] == 5
+    assert best["scatter_pages"] == 1 and main == 0.9 and gs == 0.6
+
+
+def test_choose_memory_order_scatter_competes_under_every_layout():
+    walk = (1, 1, 9, 19, 2048)
+    best, main, _ = autotune.choose(_timings({
+        walk + (2, "BS6"): 0.5, walk + (5, "BS7"): 0.7,
+        (0, 0, 9, 0, 2048, 5, "BS7"): 0.45}))
+    assert best["ball_shift"] == 19 and best["kernel_scatter"] == 5
+    assert best["scatter_pages"] == 0 and main == 0.95
+    # a walk-ordered scatter of another layout does not compete here
+    best, _, _ = autotune.choose(_timings({
+        walk + (2, "BS6"): 0.5, (2, 1, 9, 0, 2048, 5, "BS7"): 0.1}))
+    assert best["order"] == 2 and best["scatter_pages"] == 1
+
+
+def test_choose_block_kernels_keep_their_block_size():
+    best, _, _ = autotune.choose(_timings({(0, 0, 9, 0, 1024, 0, "BS6"): 0.2,
+                                           (0, 0, 9, 0, 2048, 5, "BS7"): 0.5}))
+    assert best["kernel_gather"] == 0 and best["block_nnz"] == 1024
+    assert best["kernel_scatter"] == 5 and best["scatter_pages"] == 0
