@@ -140,8 +140,10 @@ class TorchComm(Comm):
         if ops:
             for w in d.batch_isend_irecv(ops):
                 w.wait()
-        for (peer, dst), (_, h) in zip(recvs, host_recv):
-            dst.copy_(h)
+        # the uploads go on the caller's stream, ahead of the kernels that reduce them
+        with torch.cuda.stream(stream) if stream is not None else _null():
+            for (peer, dst), (_, h) in zip(recvs, host_recv):
+                dst.copy_(h)
 
 
 class _ThreadGroup:

@@ -201,7 +201,8 @@ def _torchcomm_rank(rank, world, port, path, q):
         v = torch.from_numpy(orc.uniform(o.N, case["qseed"] + 1000 * rank)).cuda()
         res = {}
         for m, name in ((O.Sym, "sym"), (O.NoTrans, "notrans"), (O.Trans, "trans")):
-            w = v.clone()
+            with torch.cuda.stream(s):
+                w = v.clone()
             o.GatherScatter(w, 1, O.Add, m, stream=s)
             s.synchronize()
             res[name] = sha(w.cpu().numpy())
