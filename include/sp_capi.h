@@ -226,6 +226,8 @@ typedef struct {
   int32_t rowOrder;   /* T rows inside a chunk: 0 CSR order, 1 grouped by size      */
   int32_t NchunksGS;  /* chunks of the gather+scatter's own walk (0: none)         */
   int32_t gsRowOrder; /* its rows: 0 CSR order, 1 grouped by size                  */
+  int32_t NpagesT;    /* pages of local columns in the main walk's order (0: none)  */
+  int32_t pageShift;  /* log2 of their size in columns                              */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

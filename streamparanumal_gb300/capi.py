@@ -48,7 +48,8 @@ class OgsInfo(ctypes.Structure):
                 ("nnzN", c_int32), ("NrowBlocksT", c_int32), ("NrowBlocksN", c_int32),
                 ("maxRowSize", c_int32), ("NgatherGlobal", c_int64), ("NchunksT", c_int32),
                 ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32),
-                ("NchunksGS", c_int32), ("gsRowOrder", c_int32)]
+                ("NchunksGS", c_int32), ("gsRowOrder", c_int32), ("NpagesT", c_int32),
+                ("pageShift", c_int32)]
 
 
 class MrInfo(ctypes.Structure):

@@ -1574,6 +1574,8 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->rowOrder = p->row_order;
   info->NchunksGS = p->nchunksGS;
   info->gsRowOrder = p->gs_grouped;
+  info->NpagesT = p->npagesT;
+  info->pageShift = p->pages_shift;
   return SP_SUCCESS;
 }
 

@@ -398,6 +398,8 @@ def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset, walk):
         ids = rng.integers(-max(2, n // 3), max(2, n // 3) + 1, n).astype(np.int64)
         ids[0] = ids[0] or 1
         h, ref = make(orc, ids)
+        assert h.info.NpagesT == (0 if walk[0] == 0 else -(-n // (1 << walk[1])))
+        assert h.info.NpagesT == 0 or h.info.pageShift == walk[1]
         rs, ci = ref["rsT"], ref["ciT"]
         g = values(orc, rs.size - 1, dtype, 17)
         base = values(orc, n, dtype, 19)
