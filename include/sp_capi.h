@@ -58,7 +58,8 @@ int32_t     sp_version(void);                 /* 10000*major + 100*minor + patch
 int64_t     sp_launch_count(void);
 void        sp_launch_count_reset(void);
 /* Tuning knobs selecting among compiled kernel variants (process-wide; the
- * autotuner's surface).  Every variant computes the same bits.  Keys:
+ * autotuner's surface).  Every variant computes the same bits, except under
+ * "reduce.norm_exact" (a different, more accurate summation of BS3).  Keys:
  *  "reduce.prefetch_chunks" (-1..64, default -1 = per-kernel defaults): L2
  *    bulk-prefetch distance of the order-exact reductions;
  *  "reduce.rolling" (1 rolling load pipeline, 0 grouped loads; default 1) for the
@@ -84,7 +85,11 @@ void        sp_launch_count_reset(void);
  *    the column-major scatter (one thread per local column); defaults 2, 2, 5;
  *  "ogs.scatter_pages" (1 = the column-major scatter takes the pages of local
  *    columns in the main walk's order when the plan has one (chunk orders 1 and 2)
- *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1).
+ *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1);
+ *  "reduce.norm_exact" (0 = the C++ platform's bs3_1 binding runs the integer-pipe
+ *    norm sp_bs3_1_fast_f64, 1 = the order-exact sp_bs3_1_f64; default 0);
+ *  "reduce.norm_ctas" (4 or 6, default 6): resident CTAs of 256 lanes per SM, and
+ *    CTAs per SM of the persistent grid, of the integer-pipe norm (values 5 run 4).
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);
@@ -172,7 +177,22 @@ sp_status sp_bs4_dot_f64_noalloc(int32_t block_size, int32_t nblocks, int64_t n,
  * FP32-storage forms accumulate in FP32 with compensated (TwoSum) per-lane
  * partials and finalise across blocks in FP64. */
 size_t    sp_reduce_scratch_bytes(void);
+/* FP64 sum of squares with the per-element work on the integer pipe: each lane
+ * accumulates the squared significands in 128-bit fixed point relative to its
+ * largest exponent (elements more than 15 binades below it, subnormals, Inf and
+ * NaN go to an FP64 fma side sum), lanes and blocks are combined in double-double.
+ * The result is within a few ulps of the exactly rounded sum for every input
+ * (Inf/NaN/overflow as FP64 gives them), hence within 1e-14 relative of the
+ * reference's order-exact bs3 (BS/BS3/okl/bs3.okl:36-41). */
 sp_status sp_norm2_f64(int64_t n, const double* a, double* out, void* scratch, sp_stream_t stream);
+/* Stage 1 of BS3 in that form, for the call sites of bs3_1 (BS/BS3/src/bs3Run.cpp:83):
+ * partial[0] = sum a*a as sp_norm2_f64 computes it and partial[1 .. nblocks) = 0,
+ * so that the unchanged stage 2 (bs3_2 = sp_reduce_finish_f64 over nblocks
+ * partials) returns partial[0].  block_size and nblocks as for sp_bs3_1_f64;
+ * scratch as above.  This is the BS3 default of the drivers and the benchmark; the
+ * order-exact sp_bs3_1_f64 stays available (knob "reduce.norm_exact"). */
+sp_status sp_bs3_1_fast_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* a,
+                            double* partial, void* scratch, sp_stream_t stream);
 sp_status sp_dot_f64(int64_t n, const double* a, const double* b, double* out, void* scratch,
                      sp_stream_t stream);
 sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch, sp_stream_t stream);

@@ -54,6 +54,8 @@ enum TuneKey : int {
   kTuneOgsGsPageShift,      // ogs plan: page size of the gather+scatter walk
   kTuneOgsGsBallShift,      // ogs plan: ball size of the gather+scatter walk
   kTuneOgsScatterPages,     // ogs column-major scatter: 1 = pages in the main walk's order
+  kTuneNormExact,           // BS3 at the drivers' bs3_1 call sites: 0 integer-pipe norm, 1 order-exact
+  kTuneNormCtas,            // integer-pipe norm: resident CTAs per SM (4 or 6)
   kTuneCount
 };
 int64_t tune(TuneKey k);

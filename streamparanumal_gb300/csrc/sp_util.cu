@@ -45,6 +45,8 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.gs_page_shift", 3, 16, {8}},
     {"ogs.gs_ball_shift", 0, 26, {18}},
     {"ogs.scatter_pages", 0, 1, {1}},
+    {"reduce.norm_exact", 0, 1, {0}},
+    {"reduce.norm_ctas", 4, 6, {6}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -14,6 +14,7 @@
 
 #include "sp_internal.h"
 #include "sp_compensated.cuh"
+#include "sp_sumsq.cuh"
 
 namespace sp {
 
@@ -604,17 +605,134 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
   finish_ticket(bv, sc, out, s);
 }
 
+// ------------------------------------------------------------------ BS3 norm on the integer pipe
+//
+// sum a*a with the per-element work on the integer pipe (sp_sumsq.cuh): a fixed
+// grid of kNormCtas CTAs per SM, U 16-byte loads per lane issued before use, one
+// fixed-point accumulator per lane, double-double across lanes and blocks in a
+// fixed order (deterministic for a given n and device), the last block to arrive
+// adds the block partials.  The result is within a few ulps of the exactly
+// rounded sum for every input.  With nzero > 1 the last block also writes
+// out[1 .. nzero) = 0, so that the reference's stage 2 (bs3_2 over nzero
+// partials, an exact sum of zeros) returns out[0] unchanged.
+
+
+__device__ __forceinline__ sumsq::DD dd_shfl_down(sumsq::DD v, int h) {
+  return sumsq::DD{__shfl_down_sync(0xffffffffu, v.hi, h),
+                   __shfl_down_sync(0xffffffffu, v.lo, h)};
+}
+
+// Double-double sum of v over the block, fixed order (valid in thread 0).
+__device__ __forceinline__ sumsq::DD block_sum_dd(sumsq::DD v, sumsq::DD* s) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) v = sumsq::dd_add(v, dd_shfl_down(v, h));
+  if (lane == 0) s[w] = v;
+  __syncthreads();
+  sumsq::DD r{0.0, 0.0};
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? s[lane] : sumsq::DD{0.0, 0.0};
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) r = sumsq::dd_add(r, dd_shfl_down(r, h));
+  }
+  __syncthreads();
+  return r;
+}
+
+// Writes the block's double-double, and lets the last block to arrive add the
+// block values in block order (lane t takes blocks t, t + 256, ..., then the fixed
+// tree) into out[0]; out[1 .. nzero) = 0.
+__device__ __forceinline__ void finish_ticket_dd(sumsq::DD bv, RedScratch sc, double* out,
+                                                 sumsq::DD* s, int nzero) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    sc.partial[2 * blockIdx.x] = bv.hi;
+    sc.partial[2 * blockIdx.x + 1] = bv.lo;
+    __threadfence();
+    const unsigned t = atomicAdd(sc.ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sumsq::DD v{0.0, 0.0};
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+    v = sumsq::dd_add(v, sumsq::DD{__ldcg(sc.partial + 2 * i), __ldcg(sc.partial + 2 * i + 1)});
+  const sumsq::DD r = block_sum_dd(v, s);
+  if (threadIdx.x == 0) {
+    out[0] = r.hi + r.lo;
+    *sc.ticket = 0u;  // leave the scratch zeroed for the next call
+  }
+  for (int i = 1 + threadIdx.x; i < nzero; i += blockDim.x) out[i] = 0.0;
+}
+
+template <int U, int CTAS>
+__global__ void __launch_bounds__(kRedThreads, CTAS)
+k_norm2_int(int64_t nvec, const double2* __restrict__ a, const double* __restrict__ as, int64_t n,
+            void* scratch, double* out, int nzero) {
+  __shared__ sumsq::DD s[kRedThreads / 32];
+  const RedScratch sc = red_scratch(scratch);
+  sumsq::Acc acc;
+  sumsq::init(acc);
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
+       base += step) {
+    double2 v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * kRedThreads;
+      v[u] = (i < nvec) ? __ldcs(a + i) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      sumsq::add(acc, v[u].x);
+      sumsq::add(acc, v[u].y);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) sumsq::add(acc, as[n - 1]);
+  finish_ticket_dd(block_sum_dd(sumsq::value(acc), s), sc, out, s, nzero);
+}
+
+// Resident CTAs per SM (knob reduce.norm_ctas: 4 or 6; the kernel fits 6 x 256
+// lanes in the register file) and the persistent grid of that many per SM.
+static unsigned norm_grid(int64_t nvec, int U, int ctas) {
+  int64_t per = (int64_t)kRedThreads * U;
+  int64_t g = (nvec + per - 1) / per;
+  int64_t cap = (int64_t)ctas * sm_count();
+  if (cap > kMaxRedBlocks) cap = kMaxRedBlocks;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+static void launch_norm2_int(int64_t n, const double* a, void* scratch, double* out, int nzero,
+                             cudaStream_t s) {
+  constexpr int U = 4;
+  const int64_t nvec = n / 2;
+  const auto* a2 = reinterpret_cast<const double2*>(a);
+  if (tune(kTuneNormCtas) == 6)
+    k_norm2_int<U, 6><<<norm_grid(nvec, U, 6), kRedThreads, 0, s>>>(nvec, a2, a, n, scratch,
+                                                                       out, nzero);
+  else
+    k_norm2_int<U, 4><<<norm_grid(nvec, U, 4), kRedThreads, 0, s>>>(nvec, a2, a, n, scratch,
+                                                                       out, nzero);
+}
+
 // FULL: x += alpha p ; r -= alpha Ap ; out = sum r*r     (FP64 storage)
 // !FULL (the reference's BS5 update): r += alpha Ap ; out = sum r*r
+// The updates are FP64 fma (bit-exact); sum r*r takes the integer-pipe
+// accumulator of the norm (one DFMA per entry fewer, within a few ulps of the
+// exactly rounded sum of the stored r).
 template <int U, bool FULL = true>
 __global__ void __launch_bounds__(kRedThreads)
 k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double2* __restrict__ Ap,
          double2* __restrict__ x, double2* __restrict__ r, const double* __restrict__ ps,
          const double* __restrict__ Aps, double* __restrict__ xs, double* __restrict__ rs,
          int64_t n, void* scratch, double* out) {
-  __shared__ double s[32];
+  __shared__ sumsq::DD s[kRedThreads / 32];
   const RedScratch sc = red_scratch(scratch);
-  double acc0 = 0.0, acc1 = 0.0;
+  sumsq::Acc acc;
+  sumsq::init(acc);
   const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
   for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
        base += step) {
@@ -646,8 +764,8 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
         nr.x = fma(ar, va[u].x, vr[u].x);
         nr.y = fma(ar, va[u].y, vr[u].y);
         __stcs(r + i, nr);
-        acc0 = fma(nr.x, nr.x, acc0);
-        acc1 = fma(nr.y, nr.y, acc1);
+        sumsq::add(acc, nr.x);
+        sumsq::add(acc, nr.y);
       }
     }
   }
@@ -656,10 +774,9 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
     if (FULL) xs[t] = fma(alpha, ps[t], xs[t]);
     const double nr = fma(FULL ? -alpha : alpha, Aps[t], rs[t]);
     rs[t] = nr;
-    acc0 = fma(nr, nr, acc0);
+    sumsq::add(acc, nr);
   }
-  const double bv = block_sum(acc0 + acc1, s);
-  finish_ticket(bv, sc, out, s);
+  finish_ticket_dd(block_sum_dd(sumsq::value(acc), s), sc, out, s, 1);
 }
 
 // FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
@@ -841,12 +958,17 @@ sp_status sp_norm2_f64(int64_t n, const double* a, double* out, void* scratch,
                        sp_stream_t stream) {
   sp_status st = check_red_args(n, scratch, out, {a}, "sp_norm2_f64");
   if (st) return st;
-  constexpr int U = 4;
-  const int64_t nvec = n / 2;
-  k_dot_f64_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
-      nvec, reinterpret_cast<const double2*>(a), reinterpret_cast<const double2*>(a), a, a, n,
-      scratch, out);
+  launch_norm2_int(n, a, scratch, out, 1, as_cuda(stream));
   return check_launch("sp_norm2_f64");
+}
+
+sp_status sp_bs3_1_fast_f64(int32_t bs, int32_t nblocks, int64_t n, const double* a,
+                            double* partial, void* scratch, sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs3_1_fast_f64");
+  if (st) return st;
+  if ((st = check_red_args(n, scratch, partial, {a}, "sp_bs3_1_fast_f64"))) return st;
+  launch_norm2_int(n, a, scratch, partial, nblocks, as_cuda(stream));
+  return check_launch("sp_bs3_1_fast_f64");
 }
 
 sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, void* scratch,

@@ -33,6 +33,9 @@ void bsVecSettings(settings_t& s) {
   s.newSetting("-fp", "--precision", "PRECISION", "FP64", "Storage precision", {"FP64", "FP32"});
   s.newSetting("-cg", "--cg-full", "CG FULL", "FALSE",
                "BS5 as the full CG update x+=alpha p, r-=alpha Ap, r.r", {"TRUE", "FALSE"});
+  s.newSetting("-ex", "--exact-norm", "EXACT NORM", "FALSE",
+               "BS3 in the reference's summation order (bit-identical; bound by the FP64 "
+               "pipe) instead of the integer-pipe norm", {"TRUE", "FALSE"});
   s.newSetting("-v", "--verbose", "VERBOSE", "FALSE", "Enable verbose output", {"TRUE", "FALSE"});
 }
 
@@ -139,6 +142,10 @@ int nblock_for(size_t N, int blockSize) {
 void bsVecRun(int which, platform_t& platform, settings_t& settings) {
   const bool fp32 = settings.compareSetting("PRECISION", "FP32");
   const bool cgFull = (which == 5) && settings.compareSetting("CG FULL", "TRUE");
+  if (which == 3)
+    checkStatus(sp_tune_set("reduce.norm_exact",
+                            settings.compareSetting("EXACT NORM", "TRUE") ? 1 : 0),
+                "EXACT NORM");
   const size_t word = fp32 ? sizeof(float) : sizeof(dfloat);
   // entries moved per DOF by each benchmark (the reference's `sc` / word size)
   const size_t perEntry[6] = {0, 2, 3, 1, 2, cgFull ? 6 : 3};

@@ -1,6 +1,8 @@
 // platform_t of the GB300 drop-in: CUDA device and stream, and the binding of the
 // reference's BS kernel names to libspgb300 entry points.
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "platform.hpp"
 
@@ -77,11 +79,37 @@ sp_status k_bs2(const Args& a, int, cudaStream_t s) {
   return sp_bs2_axpy_f64(a[0].i, a[1].d, (const double*)a[2].p, a[3].d, (double*)a[4].p,
                          (sp_stream_t)s);
 }
-// bs3.okl:27-64: (Nblocks, N, a, norm)
+// Scratch of the single-launch reductions, one per device: allocated and zeroed on
+// the first call that needs it (a driver's warm-up calls come before its timed
+// loop) and kept until exit, as the reference keeps its kernel objects
+// (libs/ogs/ogsUtils.cpp:39-43).  Every bound kernel runs on the platform's one
+// stream, so calls sharing it never overlap.
+void* reduce_scratch() {
+  static std::mutex mu;
+  static std::map<int, void*> bufs;
+  int dev = 0;
+  LIBP_CUDA_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  void*& p = bufs[dev];
+  if (!p) {
+    LIBP_CUDA_CHECK(cudaMalloc(&p, sp_reduce_scratch_bytes()));
+    LIBP_CUDA_CHECK(cudaMemset(p, 0, sp_reduce_scratch_bytes()));
+  }
+  return p;
+}
+
+// bs3.okl:27-64: (Nblocks, N, a, norm).  The integer-pipe norm by default (the
+// result lands in norm[0], norm[1..Nblocks) = 0, so bs3_2 returns it); the
+// order-exact kernel under the knob reduce.norm_exact = 1.
 sp_status k_bs3_1(const Args& a, int bs, cudaStream_t s) {
   expect(a, "bs3_1", {I, I, P, P});
-  return sp_bs3_1_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, (double*)a[3].p,
-                      (sp_stream_t)s);
+  int64_t exact = 0;
+  if (sp_status st = sp_tune_get("reduce.norm_exact", &exact)) return st;
+  if (exact)
+    return sp_bs3_1_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, (double*)a[3].p,
+                        (sp_stream_t)s);
+  return sp_bs3_1_fast_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, (double*)a[3].p,
+                           reduce_scratch(), (sp_stream_t)s);
 }
 // bs4.okl:27-65: (Nblocks, N, a, b, ddot)
 sp_status k_bs4_1(const Args& a, int bs, cudaStream_t s) {

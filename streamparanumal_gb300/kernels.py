@@ -89,6 +89,16 @@ def bs3_1(Nblocks: int, N: int, o_a, o_tmp, block_size: int = 256, stream=None) 
               _stream(stream))
 
 
+def bs3_1_fast(Nblocks: int, N: int, o_a, o_tmp, scratch: "ReduceScratch", block_size: int = 256,
+               stream=None) -> None:
+    """bs3_1 in the integer-pipe form (the drivers' default): o_tmp[0] = sum a*a,
+    o_tmp[1:Nblocks] = 0, so that bs3_2 returns o_tmp[0]."""
+    _chk(o_a, (torch.float64,), "o_a")
+    _chk(o_tmp, (torch.float64,), "o_tmp")
+    capi.call("sp_bs3_1_fast_f64", block_size, Nblocks, N, o_a.data_ptr(), o_tmp.data_ptr(),
+              scratch.ptr, _stream(stream))
+
+
 def bs4_1(Nblocks: int, N: int, o_a, o_b, o_tmp, block_size: int = 256, stream=None) -> None:
     for t, n in ((o_a, "o_a"), (o_b, "o_b"), (o_tmp, "o_tmp")):
         _chk(t, (torch.float64,), n)
@@ -125,7 +135,8 @@ class ReduceScratch:
 
 
 def norm2(o_a: torch.Tensor, o_out: torch.Tensor, scratch: ReduceScratch, stream=None) -> None:
-    """o_out[0] = sum a*a (FP64 result; compensated FP32 lanes for float32 input)."""
+    """o_out[0] = sum a*a (FP64 result: the integer-pipe sum of squares for float64
+    input, compensated FP32 lanes for float32 input)."""
     _chk(o_a, (torch.float64, torch.float32), "o_a")
     _chk(o_out, (torch.float64,), "o_out")
     fn = "sp_norm2_f64" if o_a.dtype == torch.float64 else "sp_norm2_f32"

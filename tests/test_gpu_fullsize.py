@@ -7,10 +7,17 @@ not need the oracle to run the whole workload:
   sample is exact;
 * the order-exact reductions against the oracle's restatement of the reference's
   partition on the full vectors (it runs in a few seconds with OpenMP);
-* gather+scatter against gather then scatter (the same CSR-order sums, bit for
-  bit), multiplicities from a gather of ones, and a sample of rows summed on the
-  host in CSR order from the plan's own CSR.
+* the integer-pipe BS3 norm (the drivers' default) within 1e-14 relative of the
+  order-exact result and within 4 ulps of the double-double sum, on the full
+  vector;
+* on the permuted 64^3 p = 7 box: the device-built ids and CSR equal to the
+  oracle's (the reference's min-propagation ids and ogs Setup restated, run on
+  the host with OpenMP), and BS6, BS7 and BS8 equal bit for bit to the oracle's
+  loops on the same inputs; plus gather+scatter against gather then scatter and
+  multiplicities from a gather of ones.
 """
+import hashlib
+
 import numpy as np
 import pytest
 import torch
@@ -69,14 +76,60 @@ def test_bs3_bs4_full_length_order_exact(cuda, orc):
     assert out.item() == res
 
 
+def test_bs3_fast_norm_full_length(cuda, orc):
+    ha = orc.uniform(N, 21)
+    a = torch.from_numpy(ha).cuda()
+    nb = K.nblocks_for(N, 256)
+    tmp = torch.full((256,), float("nan"), dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.bs3_1_fast(nb, N, a, tmp, K.ReduceScratch())
+    K.bs3_2(nb, tmp, out)
+    got = out.item()
+    assert torch.all(tmp[1:nb] == 0)
+    _, ref_order = orc.bs3(ha, bs=256, nblocks=nb, fmad=1)
+    assert abs(got - ref_order) <= 1e-14 * ref_order
+    exact = orc.dot_dd(ha, ha)
+    assert abs(got - exact) <= 4 * np.spacing(exact)
+
+
+def sha(x):
+    return hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest()
+
+
 def test_ogs_full_size_permuted_box(cuda, orc):
-    E, p = 64, 7
-    ids = O.box_hex_ids(E, E, E, p, 20240607, device="cuda")
+    E, p, seed = 64, 7, 20240607
+    ids = O.box_hex_ids(E, E, E, p, seed, device="cuda")
     Nt = ids.numel()
+    # ids: the device lattice formula against the oracle's min-propagation
+    hids = orc.box_hex_ids(E, E, E, p, seed)
+    assert sha(ids.cpu().numpy()) == sha(hids)
     h = O.ogs_t()
     h.Setup(Nt, ids, unique=True)
     del ids
     Ng = h.NgatherGlobal
+    # the device-built T operator against the oracle's ogs Setup (rows in order of
+    # first appearance, columns ascending: ogsSetup.cpp:492-579)
+    ref = orc.ogs_setup(hids, kind=1, unique=True)
+    del hids
+    rs, ci = h.csr(O.Trans)
+    assert sha(rs) == sha(ref["rsT"]) and sha(ci) == sha(ref["ciT"])
+    del ref
+    # BS6 / BS7 / BS8 on the full box against the oracle's loops, bit for bit
+    hq = orc.uniform(Nt, 41)
+    q = torch.from_numpy(hq).cuda()
+    gq = torch.empty(Ng, dtype=torch.float64, device="cuda")
+    h.Gather(gq, q, 1, O.Add, O.Trans)
+    want_g = orc.gather(rs, ci, hq)
+    assert sha(gq.cpu().numpy()) == sha(want_g)
+    hgv = orc.uniform(Ng, 42)
+    out = torch.zeros(Nt, dtype=torch.float64, device="cuda")
+    h.Scatter(out, torch.from_numpy(hgv).cuda(), 1, O.NoTrans)
+    assert sha(out.cpu().numpy()) == sha(orc.scatter(rs, ci, hgv, np.zeros(Nt)))
+    del out, hgv
+    h.GatherScatter(q, 1, O.Add, O.Sym)
+    assert sha(q.cpu().numpy()) == sha(orc.gather_scatter(rs, ci, rs, ci, hq))
+    del q, gq, want_g, hq, rs, ci
+    torch.cuda.empty_cache()
     assert Ng == (E * p + 1) ** 3
     # multiplicities: a gather of ones counts each row's members (1, 2, 4 or 8)
     ones = torch.ones(Nt, dtype=torch.float64, device="cuda")
@@ -94,12 +147,3 @@ def test_ogs_full_size_permuted_box(cuda, orc):
     gs = q.clone()
     h.GatherScatter(gs, 1, O.Add, O.Sym)
     assert torch.equal(gs, via)
-    # a sample of rows summed on the host in the plan's CSR order
-    rs, ci = h.csr(O.Trans)
-    hq = q.cpu().numpy()
-    hg = gq.cpu().numpy()
-    for row in np.linspace(0, Ng - 1, 20001).astype(np.int64):
-        acc = 0.0  # the reference's loop: from the op's identity, members in CSR order
-        for c in ci[rs[row]:rs[row + 1]]:
-            acc = acc + hq[c]
-        assert hg[row] == acc, row

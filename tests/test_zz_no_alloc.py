@@ -4,10 +4,12 @@ afford cudaMalloc's device-wide synchronisation), so they cannot hand over the
 partial-sum buffer that sp_bs4_1_f64 needs.  Its partials live in a static array
 of the library.
 
-Checked through the C ABI against the two-stage entry points (sp_bs4_1_f64 +
-sp_reduce_finish_f64 with a caller-allocated partial buffer): the same order-exact
-tree, so the results must agree bit for bit -- the tolerance every order-exact
-reduction test here uses.  Two calls in a row, of different sizes, show that the
+Checked through the C ABI against the oracle's restatement of the reference's
+bs4_1/bs4_2 (the same partition and tree, with the CUDA mode's fma) and against
+the two-stage entry points (sp_bs4_1_f64 + sp_reduce_finish_f64 with a
+caller-allocated partial buffer): the results must agree bit for bit -- the
+tolerance every order-exact reduction test here uses.  Two calls in a row, the
+second with fewer blocks than the first for every block size, show that the
 shared array carries nothing from one call into the next.  This file is collected
 last so that a run stopping at the first failure has run every other test."""
 import pytest
@@ -33,15 +35,18 @@ def nblocks(n, bs):
 @pytest.mark.parametrize("bs", [256, 1024])
 def test_noalloc_dot_matches_two_stage_dot_on_consecutive_calls(cuda, orc, bs):
     stream = torch.cuda.current_stream().cuda_stream
-    for n, seed in ((1_000_003, 5), (70_001, 9)):   # two calls in a row
-        a = torch.from_numpy(orc.uniform(n, seed)).cuda()
-        b = torch.from_numpy(orc.uniform(n, seed + 1)).cuda()
+    # two calls in a row; the second has fewer blocks (20,001 < 256 * 256 entries)
+    for n, seed in ((1_000_003, 5), (20_001, 9)):
+        ha, hb = orc.uniform(n, seed), orc.uniform(n, seed + 1)
+        a, b = torch.from_numpy(ha).cuda(), torch.from_numpy(hb).cuda()
         nb = nblocks(n, bs)
         got = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
         capi.call("sp_bs4_dot_f64_noalloc", bs, nb, n, a.data_ptr(), b.data_ptr(),
                   got.data_ptr(), stream)
         want = two_stage(bs, nb, n, a, b, stream)
         torch.cuda.synchronize()
+        _, ref = orc.bs4(ha, hb, bs=bs, nblocks=nb, fmad=1)
+        assert got.item() == ref
         assert got.item() == want.item()
 
 
