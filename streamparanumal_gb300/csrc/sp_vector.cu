@@ -10,7 +10,9 @@
 //   bs5:  r + alpha*Ap       -> fma(alpha, Ap, r);  acc += r*r -> fma(r, r, acc)
 #include <cstdint>
 #include <initializer_list>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "sp_internal.h"
 #include "sp_compensated.cuh"
@@ -574,7 +576,8 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
                void* scratch, double* out) {
   __shared__ double s[32];
   const RedScratch sc = red_scratch(scratch);
-  float sum = 0.f, comp = 0.f;
+  // two independent compensated sums (lanes .x/.y and .z/.w) halve the FADD chain
+  float sum = 0.f, comp = 0.f, sum1 = 0.f, comp1 = 0.f;
   const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
   for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
        base += step) {
@@ -593,15 +596,15 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       dot2_step(va[u].x, vb[u].x, sum, comp);
+      dot2_step(va[u].z, vb[u].z, sum1, comp1);
       dot2_step(va[u].y, vb[u].y, sum, comp);
-      dot2_step(va[u].z, vb[u].z, sum, comp);
-      dot2_step(va[u].w, vb[u].w, sum, comp);
+      dot2_step(va[u].w, vb[u].w, sum1, comp1);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     for (int64_t t = nvec * 4; t < n; ++t) dot2_step(as[t], bs[t], sum, comp);
   }
-  const double bv = block_sum((double)sum + (double)comp, s);
+  const double bv = block_sum(((double)sum + (double)comp) + ((double)sum1 + (double)comp1), s);
   finish_ticket(bv, sc, out, s);
 }
 
@@ -789,7 +792,7 @@ k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* 
          void* scratch, double* out) {
   __shared__ double s[32];
   const RedScratch sc = red_scratch(scratch);
-  float sum = 0.f, comp = 0.f;
+  float sum = 0.f, comp = 0.f, sum1 = 0.f, comp1 = 0.f;
   const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
   for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
        base += step) {
@@ -826,9 +829,9 @@ k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* 
         nr.w = fmaf(ar, va[u].w, vr[u].w);
         __stcs(r + i, nr);
         dot2_step(nr.x, nr.x, sum, comp);
+        dot2_step(nr.z, nr.z, sum1, comp1);
         dot2_step(nr.y, nr.y, sum, comp);
-        dot2_step(nr.z, nr.z, sum, comp);
-        dot2_step(nr.w, nr.w, sum, comp);
+        dot2_step(nr.w, nr.w, sum1, comp1);
       }
     }
   }
@@ -840,14 +843,36 @@ k_cg_f32(int64_t nvec, float alpha, const float4* __restrict__ p, const float4* 
       dot2_step(nr, nr, sum, comp);
     }
   }
-  const double bv = block_sum((double)sum + (double)comp, s);
+  const double bv = block_sum(((double)sum + (double)comp) + ((double)sum1 + (double)comp1), s);
   finish_ticket(bv, sc, out, s);
 }
 
-static unsigned red_grid(int64_t nvec, int U) {
+// CTAs of `kernel` (kRedThreads lanes each) that one SM holds at once, per device.
+static int resident_ctas(const void* kernel) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find({kernel, dev});
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kRedThreads, 0) != cudaSuccess ||
+      nb < 1) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  cache[{kernel, dev}] = nb;
+  return nb;
+}
+
+// Persistent grid of the single-launch reductions: as many CTAs as the SMs hold at
+// once (no CTA waits for a second wave while the others stream), at most one CTA
+// per U*kRedThreads vectors, at most kMaxRedBlocks.
+static unsigned red_grid(const void* kernel, int64_t nvec, int U) {
   int64_t per = (int64_t)kRedThreads * U;
   int64_t g = (nvec + per - 1) / per;
-  int64_t cap = 8 * (int64_t)sm_count();
+  int64_t cap = (int64_t)resident_ctas(kernel) * sm_count();
   if (cap > kMaxRedBlocks) cap = kMaxRedBlocks;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
@@ -948,7 +973,8 @@ sp_status sp_dot_f64(int64_t n, const double* a, const double* b, double* out, v
   if (st) return st;
   constexpr int U = 4;
   const int64_t nvec = n / 2;
-  k_dot_f64_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_dot_f64_fast<U><<<red_grid((const void*)k_dot_f64_fast<U>, nvec, U), kRedThreads, 0,
+                      as_cuda(stream)>>>(
       nvec, reinterpret_cast<const double2*>(a), reinterpret_cast<const double2*>(b), a, b, n,
       scratch, out);
   return check_launch("sp_dot_f64");
@@ -977,7 +1003,8 @@ sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, voi
   if (st) return st;
   constexpr int U = 4;
   const int64_t nvec = n / 4;
-  k_dot_f32_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_dot_f32_fast<U><<<red_grid((const void*)k_dot_f32_fast<U>, nvec, U), kRedThreads, 0,
+                      as_cuda(stream)>>>(
       nvec, reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b), a, b, n,
       scratch, out);
   return check_launch("sp_dot_f32");
@@ -989,7 +1016,8 @@ sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch,
   if (st) return st;
   constexpr int U = 4;
   const int64_t nvec = n / 4;
-  k_dot_f32_fast<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_dot_f32_fast<U><<<red_grid((const void*)k_dot_f32_fast<U>, nvec, U), kRedThreads, 0,
+                      as_cuda(stream)>>>(
       nvec, reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(a), a, a, n,
       scratch, out);
   return check_launch("sp_norm2_f32");
@@ -1001,7 +1029,8 @@ sp_status sp_cg_update_f64(int64_t n, double alpha, const double* p, const doubl
   if (st) return st;
   constexpr int U = 2;
   const int64_t nvec = n / 2;
-  k_cg_f64<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_cg_f64<U><<<red_grid((const void*)k_cg_f64<U>, nvec, U), kRedThreads, 0,
+                as_cuda(stream)>>>(
       nvec, alpha, reinterpret_cast<const double2*>(p), reinterpret_cast<const double2*>(Ap),
       reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), p, Ap, x, r, n, scratch,
       rdotr);
@@ -1014,7 +1043,8 @@ sp_status sp_cg_update_f32(int64_t n, double alpha, const float* p, const float*
   if (st) return st;
   constexpr int U = 2;
   const int64_t nvec = n / 4;
-  k_cg_f32<U><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_cg_f32<U><<<red_grid((const void*)k_cg_f32<U>, nvec, U), kRedThreads, 0,
+                as_cuda(stream)>>>(
       nvec, (float)alpha, reinterpret_cast<const float4*>(p), reinterpret_cast<const float4*>(Ap),
       reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r), p, Ap, x, r, n, scratch, rdotr);
   return check_launch("sp_cg_update_f32");
@@ -1026,7 +1056,8 @@ sp_status sp_cg_update_ref_f64(int64_t n, double alpha, const double* Ap, double
   if (st) return st;
   constexpr int U = 2;
   const int64_t nvec = n / 2;
-  k_cg_f64<U, false><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_cg_f64<U, false><<<red_grid((const void*)k_cg_f64<U, false>, nvec, U), kRedThreads, 0,
+                       as_cuda(stream)>>>(
       nvec, alpha, nullptr, reinterpret_cast<const double2*>(Ap), nullptr,
       reinterpret_cast<double2*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr);
   return check_launch("sp_cg_update_ref_f64");
@@ -1038,7 +1069,8 @@ sp_status sp_cg_update_ref_f32(int64_t n, double alpha, const float* Ap, float* 
   if (st) return st;
   constexpr int U = 2;
   const int64_t nvec = n / 4;
-  k_cg_f32<U, false><<<red_grid(nvec, U), kRedThreads, 0, as_cuda(stream)>>>(
+  k_cg_f32<U, false><<<red_grid((const void*)k_cg_f32<U, false>, nvec, U), kRedThreads, 0,
+                       as_cuda(stream)>>>(
       nvec, (float)alpha, nullptr, reinterpret_cast<const float4*>(Ap), nullptr,
       reinterpret_cast<float4*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr);
   return check_launch("sp_cg_update_ref_f32");

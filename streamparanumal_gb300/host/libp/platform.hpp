@@ -8,6 +8,7 @@
 
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "core.hpp"
@@ -74,7 +75,29 @@ class properties_t {
   std::map<std::string, std::string> kv_;
 
  public:
-  std::string& operator[](const std::string& key) { return kv_[key]; }
+  // One entry, assignable from text or a number as the reference's occa::json
+  // entries are (kernelInfo["defines/" "p_blockSize"] = blockSize in bs3Setup.cpp:39).
+  class value {
+    std::string& s_;
+
+   public:
+    explicit value(std::string& s) : s_(s) {}
+    value& operator=(const std::string& v) {
+      s_ = v;
+      return *this;
+    }
+    value& operator=(const char* v) {
+      s_ = v;
+      return *this;
+    }
+    template <typename T, typename = std::enable_if_t<std::is_arithmetic<T>::value>>
+    value& operator=(T v) {
+      s_ = std::to_string(v);
+      return *this;
+    }
+    operator const std::string&() const { return s_; }
+  };
+  value operator[](const std::string& key) { return value(kv_[key]); }
   bool has(const std::string& key) const { return kv_.count(key) != 0; }
   std::string get(const std::string& key, const std::string& dflt = "") const {
     auto it = kv_.find(key);
@@ -122,6 +145,20 @@ class kernel_t {
   cudaStream_t stream_ = nullptr;
 };
 
+// The platform's device (the reference's device_t wrapper around occa::device,
+// include/platform.hpp:66): this build runs OCCA's CUDA mode only.
+class device_t {
+  cudaStream_t* stream_ = nullptr;
+
+ public:
+  device_t() = default;
+  explicit device_t(cudaStream_t* s) : stream_(s) {}
+  std::string mode() const { return "CUDA"; }
+  void finish() const {
+    if (stream_ && *stream_) LIBP_CUDA_CHECK(cudaStreamSynchronize(*stream_));
+  }
+};
+
 class platform_t {
   struct state {
     settings_t* settings = nullptr;
@@ -133,6 +170,7 @@ class platform_t {
 
  public:
   comm_t comm;
+  device_t device;
   platform_t() = default;
   explicit platform_t(settings_t& settings);
 

@@ -41,6 +41,7 @@ platform_t::platform_t(settings_t& settings) : st_(std::make_shared<state>()) {
              st_->device < 0 || st_->device >= ndev);
   LIBP_CUDA_CHECK(cudaSetDevice(st_->device));
   LIBP_CUDA_CHECK(cudaStreamCreateWithFlags(&st_->stream, cudaStreamNonBlocking));
+  device = device_t(&st_->stream);
   st_->props["defines/dfloat"] = "double";
   st_->props["defines/dlong"] = "int";
 }

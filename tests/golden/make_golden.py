@@ -10,7 +10,7 @@ checked against the reference's own owners.  The multi-rank cases run the
 reference on several forked ranks that meet through the MPI stand-in of
 oracle/ref/shim/mpi.h.
 
-Needs the reference tree (build with `make -C oracle/ref`); the committed fixtures
+Needs the reference tree (build with `make -C oracle/ref REF=<reference tree>`); the committed fixtures
 are what the tests read.  Usage: python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -131,7 +131,7 @@ def bs_case(n, seed):
 
 def main():
     if not REFDUMP.exists():
-        sys.exit("oracle/_ref/refdump missing: run `make -C oracle/ref` with the reference tree")
+        sys.exit("oracle/_ref/refdump missing: run `make -C oracle/ref REF=<reference tree>`")
     for c in OGS_CASES:
         ogs_case(*c)
     for c in BS_CASES:
