@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--batch-emax", type=int, default=40)
     ap.add_argument("--kernels-only", action="store_true",
                     help="time the suite only (no e2e, BS0, clock soak or CPU leg): for ncu")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip detail.batch and detail.degree_sample of the default run")
+    ap.add_argument("--sample-degrees", default="1,3,7,15",
+                    help="degrees of detail.degree_sample")
     return ap.parse_args()
 
 
@@ -298,6 +302,18 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
     N = 1 << args.nlog2
     mesh, p = args.mesh, args.p
+    # ---- the batched workload and a degree sample (one GPU, outside the timed
+    # region, before the suite's buffers exist; everything they allocate is freed)
+    extras = {}
+    if world == 1 and not args.kernels_only and not args.no_extras:
+        peak0, _ = measured_peak()
+        t_x = time.time()
+        extras["degree_sample"] = degree_sample(dev, _degrees(args.sample_degrees),
+                                                args.sweep_nodes, args.perm_seed, peak0)
+        extras["batch"] = {"small": batch_measure(dev, args.batch_count, 6, args.seed, 20),
+                           "full": batch_measure(dev, args.batch_count, args.batch_emax,
+                                                 args.seed, 10)}
+        extras["extras_s"] = round(time.time() - t_x, 1)
     # ---- inputs (host, pinned) and plans
     t_setup = time.time()
     h_a = torch.from_numpy(orc.uniform(N, args.seed)).pin_memory()
@@ -530,7 +546,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "clocks": clocks,
         "detail": {"per_kernel": detail, "bs0_us_per_launch": bs0,
                    "storage_forms": forms, "setup_s": round(t_setup, 2),
-                   "mesh_and_plan_s": round(t_plan, 2), "ogs_tuning": tuning},
+                   "mesh_and_plan_s": round(t_plan, 2), "ogs_tuning": tuning, **extras},
     }
     if not args.no_cpu_baseline:
         gbs, desc, cores, _, _ = cpu_sample(args.cpu_nlog2, args.cpu_mesh, p, args.perm_seed,
@@ -714,31 +730,28 @@ def bs0_latency(stream, dev) -> dict:
     return {"plain": round(plain, 3), "graph": round(graph, 3), "launches": n}
 
 
-def run_batch(args, local_rank: int) -> None:
+def batch_measure(dev, count: int, emax: int, seed: int, reps: int) -> dict:
     """Batched uneven workload: instance i has an Ex*Ey*Ez hex box (each in
     [2, emax]) of degree p in [2, 9] (seeded), a CG update on its own x, r, p, Ap
     (n = its local nodes) and a BS8 gather+scatter on its own q.  Timed four ways:
     per-instance launches (2 per instance), the same launches replayed from one CUDA
-    graph, one persistent batched launch, and that launch replayed from a graph."""
+    graph, one persistent batched launch, and that launch replayed from a graph; in
+    FP64 and in FP32 storage.  Returns per-instance microseconds and rates."""
     import numpy as np
     import torch
 
-    from streamparanumal_gb300 import _build, batch, capi, kernels
+    from streamparanumal_gb300 import batch, capi, kernels
     from streamparanumal_gb300 import ogs as O
 
-    _build.build_library()
-    capi.load()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    rng = np.random.default_rng(args.seed)
+    rng = np.random.default_rng(seed)
     gen = torch.Generator(device=dev)
-    gen.manual_seed(args.seed)
+    gen.manual_seed(seed)
     stream = torch.cuda.Stream(device=dev)
     t0 = time.time()
     plans, vecs, alphas, sizes = [], [], [], []
     with torch.cuda.stream(stream):
-        for i in range(args.batch_count):
-            ex, ey, ez = (int(v) for v in rng.integers(2, args.batch_emax + 1, size=3))
+        for i in range(count):
+            ex, ey, ez = (int(v) for v in rng.integers(2, emax + 1, size=3))
             p = int(rng.integers(2, 10))
             ids = O.box_hex_ids(ex, ey, ez, p, int(rng.integers(1, 1 << 30)), device=dev,
                                 stream=stream)
@@ -757,11 +770,8 @@ def run_batch(args, local_rank: int) -> None:
     setup_s = time.time() - t0
     sc = kernels.ReduceScratch(dev)
     sptr = stream.cuda_stream
-    reps = max(3, min(args.steps, 20))
 
     def time_forms(vs, f32: bool) -> dict:
-        """Per-instance launches, the same launches from one graph, the batched
-        persistent launch, and that launch from a graph."""
         cg = "sp_cg_update_f32" if f32 else "sp_cg_update_f64"
         ty = capi.FLOAT if f32 else capi.DOUBLE
 
@@ -790,6 +800,7 @@ def run_batch(args, local_rank: int) -> None:
     res = time_forms(vecs, False)
     vecs32 = [{k: (t if k == "rr" else t.float()) for k, t in v.items()} for v in vecs]
     res32 = time_forms(vecs32, True)
+    del vecs32
     nodes = sum(x[4] for x in sizes)
     ng = sum(x[5] for x in sizes)
     # CG: x, p, r, Ap read, x, r written; BS8: row starts, column ids, q read and written
@@ -797,28 +808,95 @@ def run_batch(args, local_rank: int) -> None:
     nbytes32 = 24 * nodes + (ng + len(sizes)) * 4 + nodes * 4 + 8 * nodes
     per = {k: round(v / len(sizes) * 1e3, 3) for k, v in res.items()}  # us per instance
     per32 = {k: round(v / len(sizes) * 1e3, 3) for k, v in res32.items()}
+    out = {"instances": len(sizes), "Exyz_range": [2, emax], "p_range": [2, 9],
+           "local_nodes": nodes, "global_nodes": ng, "reps": reps,
+           "per_instance_us": per,
+           "speedup_batched_graph_vs_launches": round(res["per_instance_launches"]
+                                                      / res["batched_graph"], 3),
+           "GBps_batched": round(nbytes / 1e6 / res["batched_persistent"], 1),
+           "GBps_per_instance_launches": round(nbytes / 1e6 / res["per_instance_launches"], 1),
+           "fp32_storage": {
+               "per_instance_us": per32,
+               "speedup_batched_graph_vs_launches": round(res32["per_instance_launches"]
+                                                          / res32["batched_graph"], 3),
+               "GBps_batched": round(nbytes32 / 1e6 / res32["batched_persistent"], 1),
+               "useful_speedup_vs_fp64_batched": round(res["batched_persistent"]
+                                                       / res32["batched_persistent"], 3)},
+           "launches": {"per_instance": 2 * len(sizes), "batched": 1},
+           "setup_s": round(setup_s, 1)}
+    for h in plans:
+        h.Free()
+    del plans, vecs
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_batch(args, local_rank: int) -> None:
+    """--batch: batch_measure() at the command line's count and box range, one JSON line."""
+    import torch
+
+    from streamparanumal_gb300 import _build, capi
+
+    _build.build_library()
+    capi.load()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    d = batch_measure(dev, args.batch_count, args.batch_emax, args.seed,
+                      max(3, min(args.steps, 20)))
     line = {"metric": "batched CG update + BS8 per-instance time", "unit": "us/instance",
-            "value": per["batched_graph"], "higher_is_better": False, "n_gpus": 1,
-            "steps": reps, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"{len(sizes)} instances, Ex,Ey,Ez in [2,{args.batch_emax}], "
-                                   f"p in [2,9]", "local_nodes": nodes, "global_nodes": ng},
-            "per_instance_us": per,
-            "speedup_batched_graph_vs_launches": round(res["per_instance_launches"]
-                                                       / res["batched_graph"], 3),
-            "GBps_batched": round(nbytes / 1e6 / res["batched_persistent"], 1),
-            "GBps_per_instance_launches": round(nbytes / 1e6 / res["per_instance_launches"], 1),
-            "fp32_storage": {
-                "per_instance_us": per32,
-                "speedup_batched_graph_vs_launches": round(res32["per_instance_launches"]
-                                                           / res32["batched_graph"], 3),
-                "GBps_batched": round(nbytes32 / 1e6 / res32["batched_persistent"], 1),
-                "useful_speedup_vs_fp64_batched": round(res["batched_persistent"]
-                                                        / res32["batched_persistent"], 3)},
-            "launches": {"per_instance": 2 * len(sizes), "batched": 1},
-            "setup_s": round(setup_s, 1)}
+            "value": d["per_instance_us"]["batched_graph"], "higher_is_better": False,
+            "n_gpus": 1, "steps": d["reps"], "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"{d['instances']} instances, Ex,Ey,Ez in [2,{args.batch_emax}], "
+                                   f"p in [2,9]", "local_nodes": d["local_nodes"],
+                       "global_nodes": d["global_nodes"]}, **d}
     print(json.dumps(line), flush=True)
     if args.json_out:
         Path(args.json_out).write_text(json.dumps(line, indent=1))
+
+
+def degree_sample(dev, degrees, nodes: float, perm_seed: int, peak: float, reps: int = 10) -> list:
+    """BS6-BS8 per degree on a box of about `nodes` local nodes, lexicographic and
+    permuted, FP64 and FP32, with the stored per-degree tuning (as the BS6-BS8
+    drivers apply it).  GB/s by the reference accounting and the fraction of the
+    HBM peak."""
+    import torch
+
+    from streamparanumal_gb300 import autotune
+    from streamparanumal_gb300 import ogs as O
+
+    stream = torch.cuda.current_stream(dev)
+    rows = []
+    for p in degrees:
+        E = int(round((nodes / (p + 1) ** 3) ** (1.0 / 3.0)))
+        for perm in (0, perm_seed):
+            tuning = autotune.apply(p, bool(perm))
+            ids = O.box_hex_ids(E, E, E, p, perm, device=dev)
+            h = O.ogs_t()
+            h.Setup(ids.numel(), ids, unique=True)
+            Nt, Ng = ids.numel(), h.NgatherGlobal
+            del ids
+            row = {"p": p, "E": E, "layout": "permuted" if perm else "lexicographic",
+                   "local_nodes": Nt, "global_nodes": Ng, "tuning": tuning}
+            for dt, val in ((torch.float64, 8), (torch.float32, 4)):
+                q = (torch.rand(Nt, dtype=torch.float64, device=dev) * 2 - 1).to(dt)
+                gq = torch.zeros(Ng, dtype=dt, device=dev)
+                by = bytes_ogs(Nt, Ng, val)
+                by64 = bytes_ogs(Nt, Ng, 8)
+                t6 = _time(lambda: h.Gather(gq, q, 1, O.Add, O.Trans), stream, reps)
+                t7 = _time(lambda: h.Scatter(q, gq, 1, O.NoTrans), stream, reps)
+                t8 = _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), stream, reps)
+                row["fp64" if val == 8 else "fp32"] = {
+                    k: {"ms": round(t, 4), "GBps": round(by[k] / 1e6 / t, 1),
+                        "useful_GBps": round(by64[k] / 1e6 / t, 1),
+                        "frac": round(by[k] / 1e6 / t / peak, 4)}
+                    for k, t in (("BS6", t6), ("BS7", t7), ("BS8", t8))}
+                del q, gq
+            h.Free()
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            rows.append(row)
+    return rows
 
 
 def _degrees(spec: str) -> list[int]:

@@ -896,6 +896,112 @@ k_ogssp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t*
   }
 }
 
+// ------------------------------------------------------------------ lane-segmented chunks
+//
+// Kernel 6, for plans whose rows hold at most kLaneRowMax (8) members -- every hex
+// mesh.  Lane l of a warp takes the entries [8l, 8l + 8) of its chunk in CSR
+// order (build_lanes), so a row lies in one lane or crosses into the next, and
+// every lane with entries begins a row.  Nothing goes through shared memory:
+//   1. the lane loads its 8 column ids (the u-th loads of a warp are one
+//      contiguous run) and issues its 8 gathers;
+//   2. it combines the rows that begin in it, member by member from the op's
+//      identity; the partial of a row still open at its last entry goes to the
+//      next lane with one shuffle, and that lane continues it with its leading
+//      entries -- every row is combined in CSR order, the reference's order
+//      (ogsKernels.okl:64-67), so the bits are those of the other kernels;
+//   3. a backward pass gives each entry the value of its row's last entry (a
+//      second shuffle brings back the value of a row finished in the next lane);
+//      the gather writes each row once, the gather+scatter writes every member.
+// Persistent warps walk chunks c, c + W, ...; the next chunk's descriptor loads
+// ahead.  With no staging the kernel needs few registers, so more warps (more
+// gathers in flight) fit on an SM.
+template <typename T, int OP, int MODE, int PERM>  // MODE 0: gather+scatter, 1: gather
+__global__ void __launch_bounds__(kOgsThreads, kOgsLaneCtas)
+k_ogsl_gather(const int4* __restrict__ desc, int32_t nchunks, const int32_t* __restrict__ col,
+              const uint8_t* __restrict__ start, T* v, T* __restrict__ gv,
+              const int32_t* __restrict__ perm) {
+  using O = Op<T, OP>;
+  const int lane = threadIdx.x & 31;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  if (c >= nchunks) return;  // the whole warp leaves together
+  int4 d = __ldg(desc + c);
+  while (true) {
+    const int4 dn = (c + W < nchunks) ? __ldg(desc + c + W) : make_int4(0, 0, 0, 0);
+    const int32_t n = d.z, nl = (n + kLaneEntries - 1) / kLaneEntries;
+    const int nv = min(kLaneEntries, n - kLaneEntries * lane);  // <= 0: no entries here
+    const uint32_t mask = (nv > 0) ? (uint32_t)__ldg(start + (int64_t)32 * c + lane) : 0u;
+    int32_t cl[kLaneEntries];
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u)
+      cl[u] = (u < nv) ? __ldg(col + d.y + u * nl + lane) : 0;
+    T x[kLaneEntries];
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u)
+      if (u < nv) x[u] = v[cl[u]];
+    // entries before the first row start continue the previous lane's last row
+    const int first = mask ? __ffs(mask) - 1 : kLaneEntries;
+    const int lead = min(first, max(nv, 0));
+    T acc = O::init();
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u) {
+      if (u < nv && u >= first) {
+        if ((mask >> u) & 1u) acc = O::first(x[u]);
+        else O::apply(acc, x[u]);
+        x[u] = acc;  // the row's value up to entry u
+      }
+    }
+    T carry = __shfl_up_sync(0xffffffffu, acc, 1);
+#pragma unroll
+    for (int u = 0; u < kLaneEntries; ++u) {
+      if (u < lead) {
+        O::apply(carry, x[u]);
+        x[u] = carry;
+      }
+    }
+    // value of the previous lane's last row (finished in this lane's leading entries)
+    T lead_end = x[0];
+#pragma unroll
+    for (int u = 1; u < kLaneEntries; ++u)
+      if (u == lead - 1) lead_end = x[u];
+    T last = x[0];
+#pragma unroll
+    for (int u = 1; u < kLaneEntries; ++u)
+      if (u < nv) last = x[u];
+    const T from_next = __shfl_down_sync(0xffffffffu, lead_end, 1);
+    const bool next_leads = __shfl_down_sync(0xffffffffu, lead > 0 ? 1 : 0, 1) != 0 && lane < 31;
+    // rows of the chunk before this lane's first row start: an exclusive scan
+    int32_t rows_before = __popc(mask);
+#pragma unroll
+    for (int h = 1; h < 32; h <<= 1) {
+      const int32_t t = __shfl_up_sync(0xffffffffu, rows_before, h);
+      if (lane >= h) rows_before += t;
+    }
+    rows_before -= __popc(mask);
+    // backward: each entry takes its row's value (the value at the row's last entry)
+    T cur = next_leads ? from_next : last;
+#pragma unroll
+    for (int u = kLaneEntries - 1; u >= 0; --u) {
+      if (u < nv) {
+        if (u + 1 < nv && ((mask >> (u + 1)) & 1u)) cur = x[u];
+        x[u] = cur;
+        if (MODE == 1 && ((mask >> u) & 1u)) {
+          const int32_t row = d.x + rows_before + __popc(mask & ((1u << u) - 1u));
+          gv[op_row<PERM>(perm, row)] = cur;
+        }
+      }
+    }
+    if (MODE == 0) {
+#pragma unroll
+      for (int u = 0; u < kLaneEntries; ++u)
+        if (u < nv) v[cl[u]] = x[u];
+    }
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+  }
+}
+
 static inline unsigned persistent_grid(int32_t nchunks, int ctas_per_sm = 4) {
   const int64_t want = ((int64_t)nchunks + kWarpsPerCta - 1) / kWarpsPerCta;
   const int64_t cap = (int64_t)sm_count() * ctas_per_sm;
@@ -928,6 +1034,9 @@ struct ChunkArgs {
   const int32_t* colS;  // column-order entries (T chunks only, else null)
   const uint8_t* e2s;
   const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
+  const int4* laneDesc;  // lane-segmented copy of the chunks (kernel 6), or null
+  const int32_t* laneCol;
+  const uint8_t* laneStart;
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
@@ -935,7 +1044,9 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const int32_t* ci = p->d_walkCiT ? p->d_walkCiT : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
-                   p->d_colIdsST, p->d_e2sT, p->d_permT};
+                   p->d_colIdsST, p->d_e2sT, p->d_permT,
+                   reinterpret_cast<const int4*>(p->d_laneDescT), p->d_laneColT,
+                   p->d_laneStartT};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -943,11 +1054,13 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   const int32_t* rs = p->d_rsGS ? p->d_rsGS : p->d_rowStartsT;
   const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
-                   p->gs_grouped, nullptr, nullptr, nullptr};
+                   p->gs_grouped, nullptr, nullptr, nullptr,
+                   reinterpret_cast<const int4*>(p->d_laneDescGS), p->d_laneColGS,
+                   p->d_laneStartGS};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-                   p->d_colIdsN, 0, nullptr, nullptr, nullptr};
+                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 }
 
 // ------------------------------------------------------------------ dispatch
@@ -957,8 +1070,17 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
   // a gather through a renumbered walk writes gv through perm: kernels 1, 2, 5 do
   const bool perm = MODE == 1 && a.perm;
   if (perm && (kv == 3 || kv == 4)) kv = 2;
+  if (kv == 6 && !a.laneDesc) kv = 2;  // no lane-segmented copy (a row over 8 members)
   const unsigned pg = persistent_grid(a.nchunks, kOgsPersistentCtas);
-  if (kv == 5) {
+  if (kv == 6) {
+    const unsigned lg = persistent_grid(a.nchunks, kOgsLaneCtas);
+    if (perm)
+      k_ogsl_gather<T, OP, MODE, 1><<<lg, kOgsThreads, 0, s>>>(a.laneDesc, a.nchunks, a.laneCol,
+                                                               a.laneStart, v, gv, a.perm);
+    else
+      k_ogsl_gather<T, OP, MODE, 0><<<lg, kOgsThreads, 0, s>>>(a.laneDesc, a.nchunks, a.laneCol,
+                                                               a.laneStart, v, gv, nullptr);
+  } else if (kv == 5) {
     if (perm)
       k_ogsp_gather<T, OP, MODE, 1, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
                                                                  v, gv, a.grouped, a.perm);
@@ -1219,6 +1341,14 @@ static void free_plan_device(sp_ogs_plan* p) {
   if (p->d_ciGS) cudaFree(p->d_ciGS);
   p->d_chunksGS = p->d_rsGS = p->d_ciGS = nullptr;
   p->nchunksGS = p->gs_grouped = 0;
+  int32_t* lanes32[] = {p->d_laneDescT, p->d_laneColT, p->d_laneDescGS, p->d_laneColGS};
+  for (int32_t* q : lanes32)
+    if (q) cudaFree(q);
+  if (p->d_laneStartT) cudaFree(p->d_laneStartT);
+  if (p->d_laneStartGS) cudaFree(p->d_laneStartGS);
+  p->d_laneDescT = p->d_laneColT = p->d_laneDescGS = p->d_laneColGS = nullptr;
+  p->d_laneStartT = p->d_laneStartGS = nullptr;
+  p->gs_renumbered = false;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1249,6 +1379,24 @@ static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
 // need not share the walk that suits the gathers (measured on the permuted 64^3
 // p=7 box: gathers fastest on breadth-first pages of 512 entries, gather+scatter on
 // a renumbered walk of 256-entry pages in balls of 2^18 entries).
+// Lane-segmented copy of a walk (build_lanes) when every row fits two lanes and the
+// knob ogs.lanes asks for it; the kernels fall back to the pipelined ones otherwise.
+static sp_status upload_lanes(const sp_ogs_plan* p, const std::vector<int32_t>& quads,
+                              const int32_t* rs, const int32_t* ci, int32_t** d_desc,
+                              int32_t** d_col, uint8_t** d_start, cudaStream_t s) {
+  if (tune(kTuneOgsLanes) == 0 || p->maxRowSize > kLaneRowMax || quads.empty())
+    return SP_SUCCESS;
+  std::vector<int32_t> desc, col;
+  std::vector<uint8_t> start;
+  build_lanes(quads, rs, ci, desc, col, start);
+  sp_status st;
+  if ((st = upload(desc, d_desc, s))) return st;
+  if ((st = upload(col, d_col, s))) return st;
+  if ((st = upload(start, d_start, s))) return st;
+  SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+  return SP_SUCCESS;
+}
+
 static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
   const int order = (int)tune(kTuneOgsGsOrder);
   if (order < 0 || p->nchunksT == 0) return SP_SUCCESS;
@@ -1291,6 +1439,10 @@ static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(walkCi, &p->d_ciGS, s))) return st;
   }
   p->nchunksGS = (int32_t)(quads.size() / 4);
+  p->gs_renumbered = order == 2;
+  if ((st = upload_lanes(p, quads, wrs, wci, &p->d_laneDescGS, &p->d_laneColGS,
+                         &p->d_laneStartGS, s)))
+    return st;
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
 }
@@ -1484,6 +1636,9 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       p->pages_shift = page_shift;
       if ((st = upload(pages, &p->d_pagesT, s))) return st;
     }
+    if ((st = upload_lanes(p, chunksT, wrs, wci, &p->d_laneDescT, &p->d_laneColT,
+                           &p->d_laneStartT, s)))
+      return st;
     if ((st = build_gs_walk(p, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   } else {

@@ -17,8 +17,10 @@
 //     elements more than kWin binades below Emax, subnormals, Inf and NaN are
 //     added to an FP64 side sum with fma() -- FP64 semantics for the special
 //     values, negligible weight for the rest;
-//   * each thread's sum becomes a double-double once at the end, and threads and
-//     blocks are combined in double-double in a fixed order.
+//   * the lanes of a warp are combined as integers (aligned to the warp's largest
+//     window top, then 128-bit adds), so only one lane per warp converts to a
+//     double-double -- on GB300 the FP64 pipe is too narrow to let every lane do
+//     it; warps and blocks are combined in double-double in a fixed order.
 //
 // The result is the sum of squares to about 2^-59 relative (each term's error
 // is below that, and all terms are non-negative), i.e. it is within a few units
@@ -105,6 +107,26 @@ SP_SQ_HD void add96(Acc& s, uint32_t w0, uint32_t w1, uint32_t w2) {
 #endif
 }
 
+// acc += (b3:b2:b1:b0)
+SP_SQ_HD void add128(Acc& s, uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+#if defined(__CUDA_ARCH__)
+  asm("add.cc.u32 %0, %0, %4;\n\t"
+      "addc.cc.u32 %1, %1, %5;\n\t"
+      "addc.cc.u32 %2, %2, %6;\n\t"
+      "addc.u32 %3, %3, %7;"
+      : "+r"(s.a0), "+r"(s.a1), "+r"(s.a2), "+r"(s.a3)
+      : "r"(b0), "r"(b1), "r"(b2), "r"(b3));
+#else
+  uint64_t t = (uint64_t)s.a0 + b0;
+  s.a0 = (uint32_t)t;
+  t = (uint64_t)s.a1 + b1 + (t >> 32);
+  s.a1 = (uint32_t)t;
+  t = (uint64_t)s.a2 + b2 + (t >> 32);
+  s.a2 = (uint32_t)t;
+  s.a3 += b3 + (uint32_t)(t >> 32);
+#endif
+}
+
 // Adds the square of the element with words (hi, lo), whose exponent lies s2/2
 // binades below Emax (s2 = 2 (Emax - E) <= 2 kWin < 32).
 SP_SQ_HD void add_window(Acc& s, uint32_t lo, uint32_t hi, uint32_t s2) {
@@ -136,6 +158,13 @@ SP_SQ_HD void shift_down(Acc& s, uint32_t sh) {
   s.a0 = (uint32_t)L;
 }
 
+// Moves the window top up to e20 >= s.e20 (the accumulator is shifted down; bits
+// below its last place, under 2^-94 of the new unit's square scale, are dropped).
+SP_SQ_HD void align_to(Acc& s, uint32_t e20) {
+  shift_down(s, (e20 - s.e20) >> 19);
+  s.e20 = e20;
+}
+
 SP_SQ_HD void add_outside(Acc& s, double a, uint32_t lo, uint32_t hi, uint32_t ef) {
   if (ef == kExpMask) {  // Inf or NaN: the FP64 result (Inf, or NaN)
     s.f = fma(a, a, s.f);
@@ -161,6 +190,16 @@ SP_SQ_HD void add(Acc& s, double a) {
   else add_outside(s, a, lo, hi, hi & kExpMask);
 }
 
+// a += b: both aligned to the larger window top, then added as integers; the
+// side sums are added in FP64.
+SP_SQ_HD void merge(Acc& a, Acc b) {
+  const uint32_t e = a.e20 > b.e20 ? a.e20 : b.e20;
+  align_to(a, e);
+  align_to(b, e);
+  add128(a, b.a0, b.a1, b.a2, b.a3);
+  a.f += b.f;
+}
+
 // ---------------------------------------------------------------- double-double
 struct DD {
   double hi, lo;
@@ -177,19 +216,17 @@ SP_SQ_HD DD dd_add(DD a, DD b) {
   return DD{h, e - (h - s)};
 }
 
-// The accumulator's value (plus the side sum) as a double-double.
+// The accumulator's value (plus the side sum) as a double-double: the four 32-bit
+// words are exact doubles, added in double-double (any 128-bit value).
 SP_SQ_HD DD value(const Acc& s) {
-  const uint64_t H = ((uint64_t)s.a3 << 32) | s.a2, L = ((uint64_t)s.a1 << 32) | s.a0;
   DD v{0.0, 0.0};
-  if (H | L) {
-    const double hd = (double)H;  // H < 2^63: (uint64)hd is exact
-    const double he = (double)(int64_t)(H - (uint64_t)hd);
-    const double x = hd * 0x1p64, y = fma(he, 0x1p64, (double)L);
-    const double h = x + y;
-    const double lo = y - (h - x);
+  if (s.a0 | s.a1 | s.a2 | s.a3) {
+    v = dd_add(DD{(double)s.a3 * 0x1p96, 0.0}, DD{(double)s.a2 * 0x1p64, 0.0});
+    v = dd_add(v, DD{(double)s.a1 * 0x1p32, 0.0});
+    v = dd_add(v, DD{(double)s.a0, 0.0});
     // unit of the accumulator: 2^(2 Emax - 2138), Emax >= 16
     const int k = 2 * (int)(s.e20 >> 20) - 2138;
-    v = DD{ldexp(h, k), ldexp(lo, k)};
+    v = DD{ldexp(v.hi, k), ldexp(v.lo, k)};
   }
   return dd_add(v, DD{s.f, 0.0});
 }

@@ -30,13 +30,14 @@ struct TuneEntry {
   int64_t lo, hi;
   std::atomic<int64_t> value;
 };
+// One entry per TuneKey, in the enum's order (tune(k) indexes by the key).
 static TuneEntry g_tune[kTuneCount] = {
     {"reduce.prefetch_chunks", -1, 64, {-1}},
     {"ogs.block_nnz", 256, 2048, {2048}},
-    {"ogs.kernel", 0, 5, {2}},
+    {"ogs.kernel", 0, 6, {2}},
     {"ogs.order", 0, 2, {1}},
     {"reduce.rolling", 0, 1, {1}},
-    {"ogs.kernel.gather", 0, 5, {2}},
+    {"ogs.kernel.gather", 0, 6, {2}},
     {"ogs.kernel.scatter", 0, 5, {5}},
     {"ogs.rows", 0, 1, {1}},
     {"ogs.page_shift", 3, 16, {9}},
@@ -47,6 +48,8 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.scatter_pages", 0, 1, {1}},
     {"reduce.norm_exact", 0, 1, {0}},
     {"reduce.norm_ctas", 4, 6, {6}},
+    {"reduce.norm_roll", 0, 1, {0}},
+    {"ogs.lanes", 0, 1, {1}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

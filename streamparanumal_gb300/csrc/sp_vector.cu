@@ -569,6 +569,9 @@ k_dot_f64_fast(int64_t nvec, const double2* __restrict__ a, const double2* __res
   finish_ticket(bv, sc, out, s);
 }
 
+// FP32-storage dot: compensated FP32 partials (two Dot2 chains) over a rolling load
+// pipeline (the next U vectors of both inputs load while the current ones are
+// added); FP64 across lanes and blocks.
 template <int U>
 __global__ void __launch_bounds__(kRedThreads)
 k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restrict__ b,
@@ -579,26 +582,31 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
   // two independent compensated sums (lanes .x/.y and .z/.w) halve the FADD chain
   float sum = 0.f, comp = 0.f, sum1 = 0.f, comp1 = 0.f;
   const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
-  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
-       base += step) {
-    float4 va[U], vb[U];
+  int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 ca[U], cb[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kRedThreads;
+    ca[u] = (i < nvec) ? __ldcs(a + i) : z;
+    cb[u] = (i < nvec) ? __ldcs(b + i) : z;
+  }
+  for (; base < nvec; base += step) {
+    float4 na[U], nb[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int64_t i = base + (int64_t)u * kRedThreads;
-      if (i < nvec) {
-        va[u] = __ldcs(a + i);
-        vb[u] = (b == a) ? va[u] : __ldcs(b + i);
-      } else {
-        va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-        vb[u] = va[u];
-      }
+      const int64_t i = base + step + (int64_t)u * kRedThreads;
+      na[u] = (i < nvec) ? __ldcs(a + i) : z;
+      nb[u] = (i < nvec) ? __ldcs(b + i) : z;
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      dot2_step(va[u].x, vb[u].x, sum, comp);
-      dot2_step(va[u].z, vb[u].z, sum1, comp1);
-      dot2_step(va[u].y, vb[u].y, sum, comp);
-      dot2_step(va[u].w, vb[u].w, sum1, comp1);
+      dot2_step(ca[u].x, cb[u].x, sum, comp);
+      dot2_step(ca[u].z, cb[u].z, sum1, comp1);
+      dot2_step(ca[u].y, cb[u].y, sum, comp);
+      dot2_step(ca[u].w, cb[u].w, sum1, comp1);
+      ca[u] = na[u];
+      cb[u] = nb[u];
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -623,6 +631,34 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
 __device__ __forceinline__ sumsq::DD dd_shfl_down(sumsq::DD v, int h) {
   return sumsq::DD{__shfl_down_sync(0xffffffffu, v.hi, h),
                    __shfl_down_sync(0xffffffffu, v.lo, h)};
+}
+
+// The block's sum of squares as a double-double (valid in thread 0): each warp
+// adds its lanes' accumulators as integers (aligned to the warp's largest window
+// top) and the FP64 side sums in FP64, lane 0 converts once, and thread 0 adds
+// the warps' values in warp order.
+__device__ __forceinline__ sumsq::DD block_value(sumsq::Acc acc, sumsq::DD* s) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  sumsq::align_to(acc, __reduce_max_sync(0xffffffffu, acc.e20));
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const uint32_t b0 = __shfl_down_sync(0xffffffffu, acc.a0, h);
+    const uint32_t b1 = __shfl_down_sync(0xffffffffu, acc.a1, h);
+    const uint32_t b2 = __shfl_down_sync(0xffffffffu, acc.a2, h);
+    const uint32_t b3 = __shfl_down_sync(0xffffffffu, acc.a3, h);
+    sumsq::add128(acc, b0, b1, b2, b3);
+  }
+  if (__any_sync(0xffffffffu, acc.f != 0.0)) {
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) acc.f += __shfl_down_sync(0xffffffffu, acc.f, h);
+  }
+  if (lane == 0) s[w] = sumsq::value(acc);
+  __syncthreads();
+  sumsq::DD r{0.0, 0.0};
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = sumsq::dd_add(r, s[i]);
+  __syncthreads();
+  return r;
 }
 
 // Double-double sum of v over the block, fixed order (valid in thread 0).
@@ -669,7 +705,9 @@ __device__ __forceinline__ void finish_ticket_dd(sumsq::DD bv, RedScratch sc, do
   for (int i = 1 + threadIdx.x; i < nzero; i += blockDim.x) out[i] = 0.0;
 }
 
-template <int U, int CTAS>
+// ROLL = true: the next U vectors of a lane are loaded while the current ones are
+// added (twice the registers for loads, loads always in flight).
+template <int U, int CTAS, bool ROLL>
 __global__ void __launch_bounds__(kRedThreads, CTAS)
 k_norm2_int(int64_t nvec, const double2* __restrict__ a, const double* __restrict__ as, int64_t n,
             void* scratch, double* out, int nzero) {
@@ -678,22 +716,45 @@ k_norm2_int(int64_t nvec, const double2* __restrict__ a, const double* __restric
   sumsq::Acc acc;
   sumsq::init(acc);
   const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
-  for (int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x; base < nvec;
-       base += step) {
-    double2 v[U];
+  int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x;
+  if (ROLL) {
+    double2 cur[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = base + (int64_t)u * kRedThreads;
-      v[u] = (i < nvec) ? __ldcs(a + i) : make_double2(0.0, 0.0);
+      cur[u] = (i < nvec) ? __ldcs(a + i) : make_double2(0.0, 0.0);
     }
+    for (; base < nvec; base += step) {
+      double2 nxt[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      sumsq::add(acc, v[u].x);
-      sumsq::add(acc, v[u].y);
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = base + step + (int64_t)u * kRedThreads;
+        nxt[u] = (i < nvec) ? __ldcs(a + i) : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        sumsq::add(acc, cur[u].x);
+        sumsq::add(acc, cur[u].y);
+        cur[u] = nxt[u];
+      }
+    }
+  } else {
+    for (; base < nvec; base += step) {
+      double2 v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = base + (int64_t)u * kRedThreads;
+        v[u] = (i < nvec) ? __ldcs(a + i) : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        sumsq::add(acc, v[u].x);
+        sumsq::add(acc, v[u].y);
+      }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) sumsq::add(acc, as[n - 1]);
-  finish_ticket_dd(block_sum_dd(sumsq::value(acc), s), sc, out, s, nzero);
+  finish_ticket_dd(block_value(acc, s), sc, out, s, nzero);
 }
 
 // Resident CTAs per SM (knob reduce.norm_ctas: 4 or 6; the kernel fits 6 x 256
@@ -713,12 +774,59 @@ static void launch_norm2_int(int64_t n, const double* a, void* scratch, double* 
   constexpr int U = 4;
   const int64_t nvec = n / 2;
   const auto* a2 = reinterpret_cast<const double2*>(a);
-  if (tune(kTuneNormCtas) == 6)
-    k_norm2_int<U, 6><<<norm_grid(nvec, U, 6), kRedThreads, 0, s>>>(nvec, a2, a, n, scratch,
-                                                                       out, nzero);
+  const int ctas = tune(kTuneNormCtas) == 6 ? 6 : 4;
+  const unsigned g = norm_grid(nvec, U, ctas);
+  if (ctas == 6 && tune(kTuneNormRoll))  // two vectors per lane ahead fit 6 CTAs per SM
+    k_norm2_int<2, 6, true><<<norm_grid(nvec, 2, 6), kRedThreads, 0, s>>>(nvec, a2, a, n, scratch,
+                                                                           out, nzero);
+  else if (ctas == 6)
+    k_norm2_int<U, 6, false><<<g, kRedThreads, 0, s>>>(nvec, a2, a, n, scratch, out, nzero);
+  else if (tune(kTuneNormRoll))
+    k_norm2_int<U, 4, true><<<g, kRedThreads, 0, s>>>(nvec, a2, a, n, scratch, out, nzero);
   else
-    k_norm2_int<U, 4><<<norm_grid(nvec, U, 4), kRedThreads, 0, s>>>(nvec, a2, a, n, scratch,
-                                                                       out, nzero);
+    k_norm2_int<U, 4, false><<<g, kRedThreads, 0, s>>>(nvec, a2, a, n, scratch, out, nzero);
+}
+
+// FP32-storage norm: compensated FP32 partials (Dot2 steps, two independent
+// chains) over a rolling load pipeline -- the next U vectors of a lane are in
+// flight while the current ones are summed -- on a grid of the CTAs the SMs hold
+// at once; FP64 across lanes and blocks.
+template <int U>
+__global__ void __launch_bounds__(kRedThreads, 4)
+k_norm2_f32(int64_t nvec, const float4* __restrict__ a, const float* __restrict__ as, int64_t n,
+            void* scratch, double* out) {
+  __shared__ double s[32];
+  const RedScratch sc = red_scratch(scratch);
+  float sum = 0.f, comp = 0.f, sum1 = 0.f, comp1 = 0.f;
+  const int64_t step = (int64_t)gridDim.x * kRedThreads * U;
+  int64_t base = (int64_t)blockIdx.x * kRedThreads * U + threadIdx.x;
+  float4 cur[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t i = base + (int64_t)u * kRedThreads;
+    cur[u] = (i < nvec) ? __ldcs(a + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (; base < nvec; base += step) {
+    float4 nxt[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + step + (int64_t)u * kRedThreads;
+      nxt[u] = (i < nvec) ? __ldcs(a + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      dot2_step(cur[u].x, cur[u].x, sum, comp);
+      dot2_step(cur[u].z, cur[u].z, sum1, comp1);
+      dot2_step(cur[u].y, cur[u].y, sum, comp);
+      dot2_step(cur[u].w, cur[u].w, sum1, comp1);
+      cur[u] = nxt[u];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int64_t t = nvec * 4; t < n; ++t) dot2_step(as[t], as[t], sum, comp);
+  }
+  const double bv = block_sum(((double)sum + (double)comp) + ((double)sum1 + (double)comp1), s);
+  finish_ticket(bv, sc, out, s);
 }
 
 // FULL: x += alpha p ; r -= alpha Ap ; out = sum r*r     (FP64 storage)
@@ -779,7 +887,7 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
     rs[t] = nr;
     sumsq::add(acc, nr);
   }
-  finish_ticket_dd(block_sum_dd(sumsq::value(acc), s), sc, out, s, 1);
+  finish_ticket_dd(block_value(acc, s), sc, out, s, 1);
 }
 
 // FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
@@ -1001,7 +1109,7 @@ sp_status sp_dot_f32(int64_t n, const float* a, const float* b, double* out, voi
                      sp_stream_t stream) {
   sp_status st = check_red_args(n, scratch, out, {a, b}, "sp_dot_f32");
   if (st) return st;
-  constexpr int U = 4;
+  constexpr int U = 2;
   const int64_t nvec = n / 4;
   k_dot_f32_fast<U><<<red_grid((const void*)k_dot_f32_fast<U>, nvec, U), kRedThreads, 0,
                       as_cuda(stream)>>>(
@@ -1016,10 +1124,9 @@ sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch,
   if (st) return st;
   constexpr int U = 4;
   const int64_t nvec = n / 4;
-  k_dot_f32_fast<U><<<red_grid((const void*)k_dot_f32_fast<U>, nvec, U), kRedThreads, 0,
-                      as_cuda(stream)>>>(
-      nvec, reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(a), a, a, n,
-      scratch, out);
+  k_norm2_f32<U><<<red_grid((const void*)k_norm2_f32<U>, nvec, U), kRedThreads, 0,
+                   as_cuda(stream)>>>(nvec, reinterpret_cast<const float4*>(a), a, n, scratch,
+                                      out);
   return check_launch("sp_norm2_f32");
 }
 

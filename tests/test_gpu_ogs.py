@@ -410,3 +410,96 @@ def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset, walk):
     finally:
         for k, x in old.items():
             capi.tune_set(k, x)
+
+
+LANE_KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
+              "ogs.page_shift", "ogs.ball_shift", "ogs.lanes")
+
+
+@pytest.mark.parametrize("knobs", [
+    {"ogs.order": 0}, {"ogs.order": 1}, {"ogs.order": 2, "ogs.page_shift": 6},
+    {"ogs.order": 1, "ogs.ball_shift": 12, "ogs.gs_order": 2},
+    {"ogs.order": 1, "ogs.rows": 0, "ogs.gs_order": 1},
+    {"ogs.order": 1, "ogs.lanes": 0}])
+@pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0),
+                                 (3, 3, 3, 15, 4), (1, 1, 1, 1, 0)])
+def test_lane_segmented_kernel(cuda, orc, knobs, box):
+    """Kernel 6 (lanes of 8 consecutive CSR entries, rows carried across a lane
+    boundary by a shuffle) for the gather, the gather through the N operator and the
+    gather+scatter, on every walk: the reference's bits.  With ogs.lanes = 0 the
+    plan has no lane copy and the pipelined kernel runs instead."""
+    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+    try:
+        capi.tune_set("ogs.kernel", 6)
+        capi.tune_set("ogs.kernel.gather", 6)
+        for n, v in knobs.items():
+            capi.tune_set(n, v)
+        nx, ny, nz, p, seed = box
+        ids = O.box_hex_ids(nx, ny, nz, p, seed)
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        q = orc.uniform(ids.size, 71)
+        gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+        gN = torch.zeros(ref["rsN"].size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gN, torch.from_numpy(q).cuda(), 1, O.Add, O.NoTrans)
+        np.testing.assert_array_equal(host(gN), orc.gather(ref["rsN"], ref["ciN"], q))
+        for op in (O.Add, O.Mul, O.Max, O.Min):
+            dq = torch.from_numpy(q).cuda()
+            h.GatherScatter(dq, 1, op, O.Sym)
+            np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op),
+                                          err_msg=f"op {op}")
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
+@pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
+def test_lane_segmented_kernel_types(cuda, orc, dtype, op):
+    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+    try:
+        capi.tune_set("ogs.kernel", 6)
+        capi.tune_set("ogs.kernel.gather", 6)
+        ids = O.box_hex_ids(4, 3, 5, 3, 77)
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        rng = np.random.default_rng(6)
+        if dtype == torch.float32:
+            q = rng.uniform(-1, 1, ids.size).astype(np.float32)
+            q[::37] = -0.0
+        else:
+            q = rng.integers(-9, 10, ids.size).astype(np.int32 if dtype == torch.int32 else np.int64)
+        gq = torch.zeros(rs.size - 1, dtype=dtype, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, op, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q, 1, op))
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, op, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op))
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
+
+
+def test_lane_segmented_kernel_rows_over_eight(cuda, orc):
+    """Groups of up to 20 members: no lane copy is built, kernel 6 runs as 2."""
+    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+    try:
+        capi.tune_set("ogs.kernel", 6)
+        capi.tune_set("ogs.kernel.gather", 6)
+        rng = np.random.default_rng(3)
+        ids = rng.integers(1, 600, 5000).astype(np.int64)
+        h, ref = make(orc, ids)
+        assert h.info.maxRowSize > 8
+        rs, ci = ref["rsT"], ref["ciT"]
+        q = orc.uniform(ids.size, 5)
+        dq = torch.from_numpy(q).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+        gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
