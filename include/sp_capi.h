@@ -82,21 +82,18 @@ void        sp_launch_count_reset(void);
  *    persistent warp-chunk kernels, 3 asynchronously staged gathers (cp.async) or
  *    the column-order scatter, 4 column-order pipelined gathers or the persistent
  *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch or
- *    the column-major scatter (one thread per local column), 6 (gathers only)
- *    lane-segmented gathers: each lane sums 8 consecutive CSR entries in registers
- *    and hands a row open at its end to the next lane (plans whose rows hold at
- *    most 8 members; others run 2); defaults 2, 2, 5;
- *  "ogs.lanes" (1 = plans created afterwards also hold the lane-segmented copy of
- *    their walks that kernel 6 reads, when no row exceeds 8 members; default 1);
+ *    the column-major scatter (one thread per local column), 6 (gathers only) the
+ *    pipelined gathers with each chunk's column ids staged in shared memory by TMA
+ *    bulk copy one chunk ahead; defaults 2, 2, 5;
  *  "ogs.scatter_pages" (1 = the column-major scatter takes the pages of local
  *    columns in the main walk's order when the plan has one (chunk orders 1 and 2)
  *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1);
  *  "reduce.norm_exact" (0 = the C++ platform's bs3_1 binding runs the integer-pipe
  *    norm sp_bs3_1_fast_f64, 1 = the order-exact sp_bs3_1_f64; default 0);
- *  "reduce.norm_ctas" (4 or 6, default 6): resident CTAs of 256 lanes per SM, and
+ *  "reduce.norm_ctas" (4 or 6, default 4): resident CTAs of 256 lanes per SM, and
  *    CTAs per SM of the persistent grid, of the integer-pipe norm (values 5 run 4);
  *  "reduce.norm_roll" (1 = the integer-pipe norm keeps the next loads of each lane
- *    in flight while it adds the current ones; default 0).
+ *    in flight while it adds the current ones; default 1).
  * Unknown keys or out-of-range values return SP_ERR_INVALID_ARG. */
 sp_status   sp_tune_set(const char* key, int64_t value);
 sp_status   sp_tune_get(const char* key, int64_t* value);
@@ -167,7 +164,10 @@ sp_status sp_reduce_finish_f64(int32_t block_size, int32_t nblocks, const double
  * array inside the library (8 KiB held on every GPU that loads it, until exit):
  *  - nblocks must not exceed 1024 (larger values fail with SP_ERR_SIZE);
  *  - the first call on a device looks up the array's device address (set-up);
- *    make that first call before any stream capture;
+ *    make that first call before any stream capture.  The address is kept per
+ *    device ordinal for the life of the process: after cudaDeviceReset() (which
+ *    destroys the context the address belongs to) do not call this entry point
+ *    again in that process;
  *  - every call shares the one array, so calls that overlap on the GPU (other
  *    streams, other host threads) race; serialise them on one stream;
  *  - nothing in the array has to start at zero: each call writes the partials it
@@ -255,6 +255,9 @@ typedef struct {
   int32_t gsRowOrder; /* its rows: 0 CSR order, 1 grouped by size                  */
   int32_t NpagesT;    /* pages of local columns in the main walk's order (0: none)  */
   int32_t pageShift;  /* log2 of their size in columns                              */
+  int32_t waitErrors; /* bounded device waits of this plan's kernels that gave up
+                         (kernel 6's staging waits; 0 in every correct run; reading it
+                         synchronises the device)                                  */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

@@ -57,7 +57,6 @@ enum TuneKey : int {
   kTuneNormExact,           // BS3 at the drivers' bs3_1 call sites: 0 integer-pipe norm, 1 order-exact
   kTuneNormCtas,            // integer-pipe norm: resident CTAs per SM (4 or 6)
   kTuneNormRoll,            // integer-pipe norm: 1 = rolling load pipeline
-  kTuneOgsLanes,            // ogs plan: 1 = also build the lane-segmented chunks (kernel 6)
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -896,110 +896,47 @@ k_ogssp_scatter(const int4* __restrict__ chunks, int32_t nchunks, const int32_t*
   }
 }
 
-// ------------------------------------------------------------------ lane-segmented chunks
+// ------------------------------------------------------------------ bulk copies
 //
-// Kernel 6, for plans whose rows hold at most kLaneRowMax (8) members -- every hex
-// mesh.  Lane l of a warp takes the entries [8l, 8l + 8) of its chunk in CSR
-// order (build_lanes), so a row lies in one lane or crosses into the next, and
-// every lane with entries begins a row.  Nothing goes through shared memory:
-//   1. the lane loads its 8 column ids (the u-th loads of a warp are one
-//      contiguous run) and issues its 8 gathers;
-//   2. it combines the rows that begin in it, member by member from the op's
-//      identity; the partial of a row still open at its last entry goes to the
-//      next lane with one shuffle, and that lane continues it with its leading
-//      entries -- every row is combined in CSR order, the reference's order
-//      (ogsKernels.okl:64-67), so the bits are those of the other kernels;
-//   3. a backward pass gives each entry the value of its row's last entry (a
-//      second shuffle brings back the value of a row finished in the next lane);
-//      the gather writes each row once, the gather+scatter writes every member.
-// Persistent warps walk chunks c, c + W, ...; the next chunk's descriptor loads
-// ahead.  With no staging the kernel needs few registers, so more warps (more
-// gathers in flight) fit on an SM.
-template <typename T, int OP, int MODE, int PERM>  // MODE 0: gather+scatter, 1: gather
-__global__ void __launch_bounds__(kOgsThreads, kOgsLaneCtas)
-k_ogsl_gather(const int4* __restrict__ desc, int32_t nchunks, const int32_t* __restrict__ col,
-              const uint8_t* __restrict__ start, T* v, T* __restrict__ gv,
-              const int32_t* __restrict__ perm) {
-  using O = Op<T, OP>;
-  const int lane = threadIdx.x & 31;
-  const int32_t W = gridDim.x * kWarpsPerCta;
-  int32_t c = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-  if (c >= nchunks) return;  // the whole warp leaves together
-  int4 d = __ldg(desc + c);
-  while (true) {
-    const int4 dn = (c + W < nchunks) ? __ldg(desc + c + W) : make_int4(0, 0, 0, 0);
-    const int32_t n = d.z, nl = (n + kLaneEntries - 1) / kLaneEntries;
-    const int nv = min(kLaneEntries, n - kLaneEntries * lane);  // <= 0: no entries here
-    const uint32_t mask = (nv > 0) ? (uint32_t)__ldg(start + (int64_t)32 * c + lane) : 0u;
-    int32_t cl[kLaneEntries];
-#pragma unroll
-    for (int u = 0; u < kLaneEntries; ++u)
-      cl[u] = (u < nv) ? __ldg(col + d.y + u * nl + lane) : 0;
-    T x[kLaneEntries];
-#pragma unroll
-    for (int u = 0; u < kLaneEntries; ++u)
-      if (u < nv) x[u] = v[cl[u]];
-    // entries before the first row start continue the previous lane's last row
-    const int first = mask ? __ffs(mask) - 1 : kLaneEntries;
-    const int lead = min(first, max(nv, 0));
-    T acc = O::init();
-#pragma unroll
-    for (int u = 0; u < kLaneEntries; ++u) {
-      if (u < nv && u >= first) {
-        if ((mask >> u) & 1u) acc = O::first(x[u]);
-        else O::apply(acc, x[u]);
-        x[u] = acc;  // the row's value up to entry u
-      }
-    }
-    T carry = __shfl_up_sync(0xffffffffu, acc, 1);
-#pragma unroll
-    for (int u = 0; u < kLaneEntries; ++u) {
-      if (u < lead) {
-        O::apply(carry, x[u]);
-        x[u] = carry;
-      }
-    }
-    // value of the previous lane's last row (finished in this lane's leading entries)
-    T lead_end = x[0];
-#pragma unroll
-    for (int u = 1; u < kLaneEntries; ++u)
-      if (u == lead - 1) lead_end = x[u];
-    T last = x[0];
-#pragma unroll
-    for (int u = 1; u < kLaneEntries; ++u)
-      if (u < nv) last = x[u];
-    const T from_next = __shfl_down_sync(0xffffffffu, lead_end, 1);
-    const bool next_leads = __shfl_down_sync(0xffffffffu, lead > 0 ? 1 : 0, 1) != 0 && lane < 31;
-    // rows of the chunk before this lane's first row start: an exclusive scan
-    int32_t rows_before = __popc(mask);
-#pragma unroll
-    for (int h = 1; h < 32; h <<= 1) {
-      const int32_t t = __shfl_up_sync(0xffffffffu, rows_before, h);
-      if (lane >= h) rows_before += t;
-    }
-    rows_before -= __popc(mask);
-    // backward: each entry takes its row's value (the value at the row's last entry)
-    T cur = next_leads ? from_next : last;
-#pragma unroll
-    for (int u = kLaneEntries - 1; u >= 0; --u) {
-      if (u < nv) {
-        if (u + 1 < nv && ((mask >> (u + 1)) & 1u)) cur = x[u];
-        x[u] = cur;
-        if (MODE == 1 && ((mask >> u) & 1u)) {
-          const int32_t row = d.x + rows_before + __popc(mask & ((1u << u) - 1u));
-          gv[op_row<PERM>(perm, row)] = cur;
-        }
-      }
-    }
-    if (MODE == 0) {
-#pragma unroll
-      for (int u = 0; u < kLaneEntries; ++u)
-        if (u < nv) v[cl[u]] = x[u];
-    }
-    c += W;
-    if (c >= nchunks) break;
-    d = dn;
+// TMA bulk copies global -> shared memory (cp.async.bulk, completion counted in
+// bytes on an mbarrier) and bounded waits on them.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// One bounded wait for the phase with parity `ph` to complete: true when it did.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t ph) {
+  constexpr int kMaxPolls = 1 << 22;  // each poll may suspend for a while: seconds at most
+  for (int i = 0; i < kMaxPolls; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(ph)
+        : "memory");
+    if (done) return true;
   }
+  return false;
+}
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from global
+// to this CTA's shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
 }
 
 static inline unsigned persistent_grid(int32_t nchunks, int ctas_per_sm = 4) {
@@ -1034,9 +971,7 @@ struct ChunkArgs {
   const int32_t* colS;  // column-order entries (T chunks only, else null)
   const uint8_t* e2s;
   const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
-  const int4* laneDesc;  // lane-segmented copy of the chunks (kernel 6), or null
-  const int32_t* laneCol;
-  const uint8_t* laneStart;
+  int32_t* waitErr;      // the plan's count of bounded waits that gave up
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
@@ -1044,9 +979,7 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const int32_t* ci = p->d_walkCiT ? p->d_walkCiT : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
-                   p->d_colIdsST, p->d_e2sT, p->d_permT,
-                   reinterpret_cast<const int4*>(p->d_laneDescT), p->d_laneColT,
-                   p->d_laneStartT};
+                   p->d_colIdsST, p->d_e2sT, p->d_permT, p->d_waitErr};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -1054,13 +987,123 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   const int32_t* rs = p->d_rsGS ? p->d_rsGS : p->d_rowStartsT;
   const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
-                   p->gs_grouped, nullptr, nullptr, nullptr,
-                   reinterpret_cast<const int4*>(p->d_laneDescGS), p->d_laneColGS,
-                   p->d_laneStartGS};
+                   p->gs_grouped, nullptr, nullptr, nullptr, p->d_waitErr};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr};
+}
+
+// Kernel 6: the pipelined persistent gathers of kernel 2 with the chunks' column ids
+// staged in shared memory by TMA bulk copy instead of held in registers.  A chunk's
+// ids are one contiguous run (<= 1 KiB); lane 0 copies the 16-byte aligned span
+// around it into one of two buffers of its warp one chunk ahead, completing on an
+// mbarrier, so chunk c + W's ids travel while chunk c's gathers are in flight.
+// Lanes read their 8 ids from the buffer when they issue the gathers and again
+// when the gather+scatter writes back, so the 16 id registers of kernel 2 are not
+// needed.  Row words, the combine in CSR order and the results are those of
+// kernel 2 (same bits).  Measured on GB300 it is slower than kernel 2: with 5
+// CTAs per SM the register budget of 48 spills (BS6 2.9 against 5.3 TB/s on the
+// permuted 64^3 p=7 box), and at kernel 2's 4 CTAs it reaches 4.6 TB/s -- the
+// staging costs more than the id registers it frees; it is kept as the
+// bulk-staged option, and the tuned tables do not select it.
+struct __align__(128) BulkIds {
+  int32_t ids[kWarpsPerCta][2][kWarpChunkNnz + 8];  // + 3 leading ids of the aligned span
+  unsigned long long bar[kWarpsPerCta][2];
+};
+
+// Lane 0: copy the ids of chunk d into buffer b of warp w; returns nothing, the
+// buffer holds ids[(d.z & ~3) ...] so entry i of the chunk is at (d.z & 3) + i.
+__device__ __forceinline__ void stage_ids(BulkIds& bi, int w, int b, int4 d,
+                                          const int32_t* __restrict__ ids) {
+  const int32_t a0 = d.z & ~3, a1 = (d.w + 3) & ~3;
+  const uint32_t bytes = (uint32_t)(a1 - a0) * 4u;
+  mbar_expect_tx(&bi.bar[w][b], bytes);
+  if (bytes) bulk_g2s(bi.ids[w][b], ids + a0, bytes, &bi.bar[w][b]);
+}
+
+template <typename T, int OP, int MODE, int PERM>
+__global__ void __launch_bounds__(kOgsThreads, kOgsBulkCtas)
+k_ogsb_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
+              const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped,
+              const int32_t* __restrict__ perm, int32_t* __restrict__ werr) {
+  __shared__ WarpSmem<T> sm;
+  __shared__ BulkIds bi;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t W = gridDim.x * kWarpsPerCta;
+  int32_t c = blockIdx.x * kWarpsPerCta + w;
+  if (c >= nchunks) return;  // the whole warp leaves together
+  T* sv = sm.val[w];
+  int32_t* srs = sm.rs[w];
+  uint8_t* sro = sm.ro[w];
+  if (lane == 0) {
+    mbar_init(&bi.bar[w][0]);
+    mbar_init(&bi.bar[w][1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  const int4 zero = make_int4(0, 0, 0, 0);
+  int4 d = __ldg(chunks + c);
+  int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  if (lane == 0) stage_ids(bi, w, 0, d, ids);
+  int b = 0;
+  uint32_t ph0 = 0u, ph1 = 0u;
+  while (true) {
+    const bool more = c + W < nchunks;
+    const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    // buffer b ^ 1 was last read in the previous iteration, which every lane has left
+    if (more && lane == 0) stage_ids(bi, w, b ^ 1, dn, ids);
+    if (!mbar_wait(&bi.bar[w][b], b ? ph1 : ph0)) {
+      if (lane == 0) atomicAdd(werr, 1);
+      if (more) mbar_wait(&bi.bar[w][b ^ 1], b ? ph0 : ph1);  // no copy may outlive the CTA
+      return;
+    }
+    if (b) ph1 ^= 1u;
+    else ph0 ^= 1u;
+    const int32_t* cid = bi.ids[w][b] + (d.z & 3);
+    const int32_t gn = d.w - d.z, nr = d.y - d.x;
+    T val[kOgsPerLane];
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) val[u] = v[cid[lane + 32 * u]];
+    stage_rows(rs, grouped, d, lane, srs, sro);
+#pragma unroll
+    for (int u = 0; u < kOgsPerLane; ++u)
+      if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+    __syncwarp();
+    for (int32_t r = lane; r < nr; r += 32) {
+      const RowRef q = staged_row(srs, sro, grouped, r);
+      T acc = row_combine<T, OP>(sv, q.a, q.b);
+      if (MODE == 0) {
+        for (int32_t i = q.a; i < q.b; ++i) sv[i] = acc;
+      } else {
+        gv[op_row<PERM>(perm, d.x + q.row)] = acc;
+      }
+    }
+    __syncwarp();
+    if (MODE == 0) {
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u)
+        if (lane + 32 * u < gn) v[cid[lane + 32 * u]] = sv[lane + 32 * u];
+    }
+    __syncwarp();  // buffers sv and ids[b] are refilled by the next chunks
+    c += W;
+    if (c >= nchunks) break;
+    d = dn;
+    dn = dnn;
+    b ^= 1;
+  }
+}
+
+template <typename T, int OP, int MODE>
+static void launch_bulk_gather(const ChunkArgs& a, T* v, T* gv, bool perm, cudaStream_t s) {
+  const unsigned g = persistent_grid(a.nchunks, kOgsBulkCtas);
+  if (perm)
+    k_ogsb_gather<T, OP, MODE, 1><<<g, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v,
+                                                           gv, a.grouped, a.perm, a.waitErr);
+  else
+    k_ogsb_gather<T, OP, MODE, 0><<<g, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids, v,
+                                                           gv, a.grouped, nullptr, a.waitErr);
 }
 
 // ------------------------------------------------------------------ dispatch
@@ -1070,16 +1113,10 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
   // a gather through a renumbered walk writes gv through perm: kernels 1, 2, 5 do
   const bool perm = MODE == 1 && a.perm;
   if (perm && (kv == 3 || kv == 4)) kv = 2;
-  if (kv == 6 && !a.laneDesc) kv = 2;  // no lane-segmented copy (a row over 8 members)
+  if (kv == 6 && !a.waitErr) kv = 2;  // a plan without chunks has no wait-error word
   const unsigned pg = persistent_grid(a.nchunks, kOgsPersistentCtas);
   if (kv == 6) {
-    const unsigned lg = persistent_grid(a.nchunks, kOgsLaneCtas);
-    if (perm)
-      k_ogsl_gather<T, OP, MODE, 1><<<lg, kOgsThreads, 0, s>>>(a.laneDesc, a.nchunks, a.laneCol,
-                                                               a.laneStart, v, gv, a.perm);
-    else
-      k_ogsl_gather<T, OP, MODE, 0><<<lg, kOgsThreads, 0, s>>>(a.laneDesc, a.nchunks, a.laneCol,
-                                                               a.laneStart, v, gv, nullptr);
+    launch_bulk_gather<T, OP, MODE>(a, v, gv, perm, s);
   } else if (kv == 5) {
     if (perm)
       k_ogsp_gather<T, OP, MODE, 1, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
@@ -1341,14 +1378,8 @@ static void free_plan_device(sp_ogs_plan* p) {
   if (p->d_ciGS) cudaFree(p->d_ciGS);
   p->d_chunksGS = p->d_rsGS = p->d_ciGS = nullptr;
   p->nchunksGS = p->gs_grouped = 0;
-  int32_t* lanes32[] = {p->d_laneDescT, p->d_laneColT, p->d_laneDescGS, p->d_laneColGS};
-  for (int32_t* q : lanes32)
-    if (q) cudaFree(q);
-  if (p->d_laneStartT) cudaFree(p->d_laneStartT);
-  if (p->d_laneStartGS) cudaFree(p->d_laneStartGS);
-  p->d_laneDescT = p->d_laneColT = p->d_laneDescGS = p->d_laneColGS = nullptr;
-  p->d_laneStartT = p->d_laneStartGS = nullptr;
-  p->gs_renumbered = false;
+  if (p->d_waitErr) cudaFree(p->d_waitErr);
+  p->d_waitErr = nullptr;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1361,7 +1392,9 @@ static void free_plan_device(sp_ogs_plan* p) {
 
 template <typename E>
 static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
-  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(E);
+  // 16 bytes of slack past the end: kernel 6 copies the 16-byte aligned span
+  // around a chunk's column ids, which may reach up to 12 bytes beyond the last id
+  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(E) + 16;
   if (cudaMalloc(d, bytes) != cudaSuccess) {
     cudaGetLastError();
     *d = nullptr;
@@ -1379,24 +1412,6 @@ static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
 // need not share the walk that suits the gathers (measured on the permuted 64^3
 // p=7 box: gathers fastest on breadth-first pages of 512 entries, gather+scatter on
 // a renumbered walk of 256-entry pages in balls of 2^18 entries).
-// Lane-segmented copy of a walk (build_lanes) when every row fits two lanes and the
-// knob ogs.lanes asks for it; the kernels fall back to the pipelined ones otherwise.
-static sp_status upload_lanes(const sp_ogs_plan* p, const std::vector<int32_t>& quads,
-                              const int32_t* rs, const int32_t* ci, int32_t** d_desc,
-                              int32_t** d_col, uint8_t** d_start, cudaStream_t s) {
-  if (tune(kTuneOgsLanes) == 0 || p->maxRowSize > kLaneRowMax || quads.empty())
-    return SP_SUCCESS;
-  std::vector<int32_t> desc, col;
-  std::vector<uint8_t> start;
-  build_lanes(quads, rs, ci, desc, col, start);
-  sp_status st;
-  if ((st = upload(desc, d_desc, s))) return st;
-  if ((st = upload(col, d_col, s))) return st;
-  if ((st = upload(start, d_start, s))) return st;
-  SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
-  return SP_SUCCESS;
-}
-
 static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
   const int order = (int)tune(kTuneOgsGsOrder);
   if (order < 0 || p->nchunksT == 0) return SP_SUCCESS;
@@ -1439,10 +1454,6 @@ static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(walkCi, &p->d_ciGS, s))) return st;
   }
   p->nchunksGS = (int32_t)(quads.size() / 4);
-  p->gs_renumbered = order == 2;
-  if ((st = upload_lanes(p, quads, wrs, wci, &p->d_laneDescGS, &p->d_laneColGS,
-                         &p->d_laneStartGS, s)))
-    return st;
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
 }
@@ -1631,14 +1642,15 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     for (int32_t r = 0; r < p->NrowsT; ++r)
       for (int32_t i = p->rowStartsT[r]; i < p->rowStartsT[r + 1]; ++i) rowOfCol[p->colIdsT[i]] = r;
     if ((st = upload(rowOfCol, &p->d_rowOfColT, s))) return st;
-    if (!pages.empty()) {
+    // the walk-ordered scatter stores each page it is given, so it runs only when
+    // the list holds every page of [0, N) (exactly once, as page_order emits them)
+    const int64_t npages_all = (std::max<int64_t>(p->N, 1) + (1LL << page_shift) - 1) >> page_shift;
+    if (!pages.empty() && (int64_t)pages.size() == npages_all) {
       p->npagesT = (int32_t)pages.size();
       p->pages_shift = page_shift;
       if ((st = upload(pages, &p->d_pagesT, s))) return st;
     }
-    if ((st = upload_lanes(p, chunksT, wrs, wci, &p->d_laneDescT, &p->d_laneColT,
-                           &p->d_laneStartT, s)))
-      return st;
+    if ((st = upload(std::vector<int32_t>{0}, &p->d_waitErr, s))) return st;
     if ((st = build_gs_walk(p, s))) return st;
     SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   } else {
@@ -1731,6 +1743,11 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->gsRowOrder = p->gs_grouped;
   info->NpagesT = p->npagesT;
   info->pageShift = p->pages_shift;
+  info->waitErrors = 0;
+  if (p->d_waitErr) {
+    int32_t* dev = p->d_waitErr;
+    SP_CUDA_TRY(cudaMemcpy(&info->waitErrors, dev, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
   return SP_SUCCESS;
 }
 

@@ -400,31 +400,4 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
   }
 }
 
-void build_lanes(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
-                 std::vector<int32_t>& desc, std::vector<int32_t>& col,
-                 std::vector<uint8_t>& start) {
-  const int64_t nchunks = (int64_t)quads.size() / 4;
-  desc.assign(4 * nchunks, 0);
-  start.assign(32 * nchunks, 0);
-  int64_t total = 0;
-  for (int64_t c = 0; c < nchunks; ++c) {
-    const int32_t n = quads[4 * c + 3] - quads[4 * c + 2];
-    desc[4 * c + 0] = quads[4 * c];
-    desc[4 * c + 1] = (int32_t)total;
-    desc[4 * c + 2] = n;
-    total += 8 * (int64_t)((n + 7) / 8);
-  }
-  col.assign(std::max<int64_t>(total, 1), 0);
-#pragma omp parallel for schedule(dynamic, 256)
-  for (int64_t c = 0; c < nchunks; ++c) {
-    const int32_t r0 = quads[4 * c], r1 = quads[4 * c + 1], g0 = quads[4 * c + 2];
-    const int32_t n = desc[4 * c + 2], nl = (n + 7) / 8, p0 = desc[4 * c + 1];
-    for (int32_t e = 0; e < n; ++e) col[p0 + (e % 8) * nl + e / 8] = ci[g0 + e];
-    for (int32_t r = r0; r < r1; ++r) {
-      const int32_t e = rs[r] - g0;
-      if (rs[r + 1] > rs[r]) start[32 * c + e / 8] |= (uint8_t)(1u << (e % 8));
-    }
-  }
-}
-
 }  // namespace sp

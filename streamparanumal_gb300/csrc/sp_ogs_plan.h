@@ -28,15 +28,9 @@ constexpr int kWarpsPerCta = 8;
 #define SP_OGS_SCATTER_CTAS 5
 #endif
 constexpr int kOgsPersistentCtas = SP_OGS_PERSISTENT_CTAS;
-// Lane-segmented chunks: entries per lane, the largest row they serve (a row then
-// spans at most two lanes and every lane with entries begins a row), and the
-// resident CTAs per SM the lane kernels are compiled for.
-constexpr int kLaneEntries = 8;
-constexpr int kLaneRowMax = 8;
-#ifndef SP_OGS_LANE_CTAS
-#define SP_OGS_LANE_CTAS 4
-#endif
-constexpr int kOgsLaneCtas = SP_OGS_LANE_CTAS;
+// Resident CTAs per SM of the bulk-staged pipelined gathers (kernel 6): as many
+// as kernel 2 (a fifth CTA leaves too few registers and spills).
+constexpr int kOgsBulkCtas = 4;
 constexpr int kOgsScatterCtas = SP_OGS_SCATTER_CTAS;
 
 struct OgsOperatorDev {
@@ -91,17 +85,6 @@ void build_grouped(const std::vector<int32_t>& quads, int32_t nrows, const int32
 void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_t* rowStarts,
                   const int32_t* rowsG, const int32_t* colIdsE, std::vector<int32_t>& colIdsS,
                   std::vector<uint8_t>& rowOfS, std::vector<uint8_t>& e2s);
-
-// Lane-segmented copy of a walk's chunks, for plans whose rows hold at most
-// kLaneRowMax members (the lane kernels: lane l of a warp takes entries
-// [8l, 8l + 8) of the chunk in CSR order, so a row lies in one lane or crosses into
-// the next one).  desc[4c..4c+3] = (r0, p0, n, 0): the chunk's first row, the
-// offset of its entries in `col` and their count; col[p0 + u * nl + l] is entry
-// 8l + u (nl = ceil(n / 8), so the u-th loads of a warp are one contiguous run);
-// start[32c + l] has bit u set when entry 8l + u begins a row.
-void build_lanes(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
-                 std::vector<int32_t>& desc, std::vector<int32_t>& col,
-                 std::vector<uint8_t>& start);
 
 // Element slots of an nx*ny*nz box: slot[e] is where lexicographic element e is
 // stored (identity for perm_seed 0, else a seeded Fisher-Yates shuffle).
@@ -178,15 +161,8 @@ struct sp_ogs_plan {
   int32_t gs_grouped = 0;
   int32_t* d_rsGS = nullptr;         // grouped rows, or the walk's row starts
   int32_t* d_ciGS = nullptr;         // grouped or walk column ids
-  // lane-segmented copies of the main walk's and the gather+scatter walk's chunks
-  // (build_lanes; null when a row holds more than kLaneRowMax members)
-  int32_t* d_laneDescT = nullptr;
-  int32_t* d_laneColT = nullptr;
-  uint8_t* d_laneStartT = nullptr;
-  int32_t* d_laneDescGS = nullptr;
-  int32_t* d_laneColGS = nullptr;
-  uint8_t* d_laneStartGS = nullptr;
-  bool gs_renumbered = false;        // the gather+scatter walk renumbers rows (order 2)
+  // count of bounded device waits that gave up (the bulk-staged gathers' waits)
+  int32_t* d_waitErr = nullptr;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations
   bool own_blocks_n = false;      // d_blocksN is a separate allocation
 

@@ -47,9 +47,8 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.gs_ball_shift", 0, 26, {18}},
     {"ogs.scatter_pages", 0, 1, {1}},
     {"reduce.norm_exact", 0, 1, {0}},
-    {"reduce.norm_ctas", 4, 6, {6}},
-    {"reduce.norm_roll", 0, 1, {0}},
-    {"ogs.lanes", 0, 1, {1}},
+    {"reduce.norm_ctas", 4, 6, {4}},
+    {"reduce.norm_roll", 0, 1, {1}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -202,6 +202,12 @@ class ogs_t:
                       capi.i32p(rsN), capi.i32p(ciN), _stream(stream), ctypes.byref(h))
         self._attach(h, Signed, False)
 
+    def plan_info(self) -> capi.OgsInfo:
+        """The plan's sp_ogs_info now (waitErrors reads the device: it synchronises)."""
+        info = capi.OgsInfo()
+        capi.call("sp_ogs_plan_info", self._plan, ctypes.byref(info))
+        return info
+
     def _attach(self, h, kind, unique):
         self._plan = h
         info = capi.OgsInfo()

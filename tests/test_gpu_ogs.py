@@ -412,23 +412,22 @@ def test_column_major_scatter_any_length(cuda, orc, n, dtype, offset, walk):
             capi.tune_set(k, x)
 
 
-LANE_KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
-              "ogs.page_shift", "ogs.ball_shift", "ogs.lanes")
+BULK_KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
+              "ogs.page_shift", "ogs.ball_shift")
 
 
 @pytest.mark.parametrize("knobs", [
     {"ogs.order": 0}, {"ogs.order": 1}, {"ogs.order": 2, "ogs.page_shift": 6},
     {"ogs.order": 1, "ogs.ball_shift": 12, "ogs.gs_order": 2},
-    {"ogs.order": 1, "ogs.rows": 0, "ogs.gs_order": 1},
-    {"ogs.order": 1, "ogs.lanes": 0}])
+    {"ogs.order": 1, "ogs.rows": 0, "ogs.gs_order": 1}])
 @pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0),
                                  (3, 3, 3, 15, 4), (1, 1, 1, 1, 0)])
-def test_lane_segmented_kernel(cuda, orc, knobs, box):
-    """Kernel 6 (lanes of 8 consecutive CSR entries, rows carried across a lane
-    boundary by a shuffle) for the gather, the gather through the N operator and the
-    gather+scatter, on every walk: the reference's bits.  With ogs.lanes = 0 the
-    plan has no lane copy and the pipelined kernel runs instead."""
-    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+def test_bulk_staged_gathers(cuda, orc, knobs, box):
+    """Kernel 6 (the pipelined gathers with each chunk's column ids brought to shared
+    memory by TMA bulk copy, one chunk ahead) for the gather, the gather through the
+    N operator and the gather+scatter with every op, on every walk: the reference's
+    bits, and no bounded staging wait gave up."""
+    saved = {n: capi.tune_get(n) for n in BULK_KNOBS}
     try:
         capi.tune_set("ogs.kernel", 6)
         capi.tune_set("ogs.kernel.gather", 6)
@@ -450,6 +449,7 @@ def test_lane_segmented_kernel(cuda, orc, knobs, box):
             h.GatherScatter(dq, 1, op, O.Sym)
             np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op),
                                           err_msg=f"op {op}")
+        assert h.plan_info().waitErrors == 0
     finally:
         for n, v in saved.items():
             capi.tune_set(n, v)
@@ -457,8 +457,8 @@ def test_lane_segmented_kernel(cuda, orc, knobs, box):
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
 @pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
-def test_lane_segmented_kernel_types(cuda, orc, dtype, op):
-    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+def test_bulk_staged_gathers_types(cuda, orc, dtype, op):
+    saved = {n: capi.tune_get(n) for n in BULK_KNOBS}
     try:
         capi.tune_set("ogs.kernel", 6)
         capi.tune_set("ogs.kernel.gather", 6)
@@ -477,21 +477,22 @@ def test_lane_segmented_kernel_types(cuda, orc, dtype, op):
         dq = torch.from_numpy(q.copy()).cuda()
         h.GatherScatter(dq, 1, op, O.Sym)
         np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op))
+        assert h.plan_info().waitErrors == 0
     finally:
         for n, v in saved.items():
             capi.tune_set(n, v)
 
 
-def test_lane_segmented_kernel_rows_over_eight(cuda, orc):
-    """Groups of up to 20 members: no lane copy is built, kernel 6 runs as 2."""
-    saved = {n: capi.tune_get(n) for n in LANE_KNOBS}
+def test_bulk_staged_gathers_large_groups(cuda, orc):
+    """Random ids with groups of up to ~20 members, chunks starting at every offset
+    modulo 4 (the bulk copy's 16-byte aligned span around each chunk's ids)."""
+    saved = {n: capi.tune_get(n) for n in BULK_KNOBS}
     try:
         capi.tune_set("ogs.kernel", 6)
         capi.tune_set("ogs.kernel.gather", 6)
         rng = np.random.default_rng(3)
-        ids = rng.integers(1, 600, 5000).astype(np.int64)
+        ids = rng.integers(1, 600, 5003).astype(np.int64)
         h, ref = make(orc, ids)
-        assert h.info.maxRowSize > 8
         rs, ci = ref["rsT"], ref["ciT"]
         q = orc.uniform(ids.size, 5)
         dq = torch.from_numpy(q).cuda()
@@ -500,6 +501,7 @@ def test_lane_segmented_kernel_rows_over_eight(cuda, orc):
         gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
         h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
         np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+        assert h.plan_info().waitErrors == 0
     finally:
         for n, v in saved.items():
             capi.tune_set(n, v)
