@@ -57,6 +57,7 @@ enum TuneKey : int {
   kTuneNormExact,           // BS3 at the drivers' bs3_1 call sites: 0 integer-pipe norm, 1 order-exact
   kTuneNormCtas,            // integer-pipe norm: resident CTAs per SM (4 or 6)
   kTuneNormRoll,            // integer-pipe norm: 1 = rolling load pipeline
+  kTuneOgsSingles,          // ogs kernel 2: 1 = single-member rows skip staging and combine
   kTuneCount
 };
 int64_t tune(TuneKey k);

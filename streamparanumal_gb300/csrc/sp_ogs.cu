@@ -413,14 +413,34 @@ __device__ __forceinline__ void prefetch_elem_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// Bit equality (x = first(x) for most values: then a gather+scatter need not store).
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool same_bits(float a, float b) {
+  return __float_as_int(a) == __float_as_int(b);
+}
+__device__ __forceinline__ bool same_bits(int32_t a, int32_t b) { return a == b; }
+__device__ __forceinline__ bool same_bits(long long a, long long b) { return a == b; }
+
 // PF = 1 (kernel 5): as soon as this chunk's values have landed, the next chunk's
 // values are prefetched into L2 from the column ids already in registers, so
 // they stream in while this chunk is combined and written back.
-template <typename T, int OP, int MODE, int PF = 0, int PERM = 0>  // MODE 0: gather+scatter, 1: gather
+// SG = 1 (grouped rows with the plan's singleton split, knob ogs.singles; the
+// dispatch uses it for the in-place gather+scatter): the rows of one member -- the
+// chunk's last rows, since grouped rows run largest first -- skip the staging and
+// the combine loop: the lane that gathered such a row's value applies the op's
+// first step to it (first(x), e.g. 0 + x) and stores it back only when its bits
+// changed (-0 under Add, -Inf and NaN under Max), so the memory ends the same and
+// the unchanged values are not rewritten.  (A gather through this path writes
+// each single-member row from the lane that gathered it; the row word it needs then
+// waits on the gather, which measured slower than the staged path.)
+// sing[c] = (rows of chunk c with more than one member, their entries).
+template <typename T, int OP, int MODE, int PF = 0, int PERM = 0, int SG = 0>
 __global__ void __launch_bounds__(kOgsThreads, kOgsPersistentCtas)
 k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* __restrict__ rs,
               const int32_t* __restrict__ ids, T* v, T* __restrict__ gv, int grouped,
-              const int32_t* __restrict__ perm) {
+              const int32_t* __restrict__ perm, const int2* __restrict__ sing) {
   __shared__ WarpSmem<T> sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
@@ -432,21 +452,46 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
   const int4 zero = make_int4(0, 0, 0, 0);
   int4 d = __ldg(chunks + c);
   int4 dn = (c + W < nchunks) ? __ldg(chunks + c + W) : zero;
+  int2 sg = SG ? __ldg(sing + c) : make_int2(0, 0);
   int32_t col[kOgsPerLane];
   load_cols(ids, d, lane, col);
   while (true) {
     const int4 dnn = (c + 2 * W < nchunks) ? __ldg(chunks + c + 2 * W) : zero;
+    const int2 sgn = (SG && c + W < nchunks) ? __ldg(sing + c + W) : make_int2(0, 0);
     const int32_t gn = d.w - d.z, nr = d.y - d.x;
+    // rows [0, k0) of the chunk hold entries [0, s0); the rest are single members
+    const int32_t k0 = SG ? sg.x : nr, s0 = SG ? sg.y : gn;
     T val[kOgsPerLane];
 #pragma unroll
     for (int u = 0; u < kOgsPerLane; ++u)
       if (lane + 32 * u < gn) val[u] = v[col[u]];
-    stage_rows(rs, grouped, d, lane, srs, sro);
+    if (SG) {
+      for (int32_t r = lane; r < k0; r += 32) {
+        const int32_t wd = __ldg(rs + d.x + r);
+        srs[r] = wd & 0xFFFF;
+        sro[r] = (uint8_t)(wd >> 16);
+      }
+      if (lane == 0) srs[k0] = s0;
+    } else {
+      stage_rows(rs, grouped, d, lane, srs, sro);
+    }
     int32_t coln[kOgsPerLane];
     load_cols(ids, dn, lane, coln);
 #pragma unroll
-    for (int u = 0; u < kOgsPerLane; ++u)
-      if (lane + 32 * u < gn) sv[lane + 32 * u] = val[u];
+    for (int u = 0; u < kOgsPerLane; ++u) {
+      const int32_t e = lane + 32 * u;
+      if (e < s0) {
+        sv[e] = val[u];
+      } else if (SG && e < gn) {
+        const T y = Op<T, OP>::first(val[u]);
+        if (MODE == 1) {
+          const int32_t wd = __ldg(rs + d.x + k0 + (e - s0));
+          gv[op_row<PERM>(perm, d.x + (wd >> 16))] = y;
+        } else if (!same_bits(y, val[u])) {
+          v[col[u]] = y;
+        }
+      }
+    }
     if (PF) {
       const int32_t gnn = dn.w - dn.z;
 #pragma unroll
@@ -454,7 +499,7 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
         if (lane + 32 * u < gnn) prefetch_elem_l2(v + coln[u]);
     }
     __syncwarp();
-    for (int32_t r = lane; r < nr; r += 32) {
+    for (int32_t r = lane; r < k0; r += 32) {
       const RowRef q = staged_row(srs, sro, grouped, r);
       T acc = row_combine<T, OP>(sv, q.a, q.b);
       if (MODE == 0) {
@@ -467,13 +512,14 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
     if (MODE == 0) {
 #pragma unroll
       for (int u = 0; u < kOgsPerLane; ++u)
-        if (lane + 32 * u < gn) v[col[u]] = sv[lane + 32 * u];
+        if (lane + 32 * u < s0) v[col[u]] = sv[lane + 32 * u];
       __syncwarp();
     }
     c += W;
     if (c >= nchunks) break;
     d = dn;
     dn = dnn;
+    sg = sgn;
 #pragma unroll
     for (int u = 0; u < kOgsPerLane; ++u) col[u] = coln[u];
   }
@@ -972,6 +1018,7 @@ struct ChunkArgs {
   const uint8_t* e2s;
   const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
   int32_t* waitErr;      // the plan's count of bounded waits that gave up
+  const int2* sing;      // per chunk (multi-member rows, their entries), grouped rows only
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
@@ -979,7 +1026,8 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const int32_t* ci = p->d_walkCiT ? p->d_walkCiT : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
-                   p->d_colIdsST, p->d_e2sT, p->d_permT, p->d_waitErr};
+                   p->d_colIdsST, p->d_e2sT, p->d_permT, p->d_waitErr,
+                   g ? reinterpret_cast<const int2*>(p->d_singT) : nullptr};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -987,11 +1035,12 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   const int32_t* rs = p->d_rsGS ? p->d_rsGS : p->d_rowStartsT;
   const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
-                   p->gs_grouped, nullptr, nullptr, nullptr, p->d_waitErr};
+                   p->gs_grouped, nullptr, nullptr, nullptr, p->d_waitErr,
+                   p->gs_grouped ? reinterpret_cast<const int2*>(p->d_singGS) : nullptr};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr};
+                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr, nullptr};
 }
 
 // Kernel 6: the pipelined persistent gathers of kernel 2 with the chunks' column ids
@@ -1119,11 +1168,11 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
     launch_bulk_gather<T, OP, MODE>(a, v, gv, perm, s);
   } else if (kv == 5) {
     if (perm)
-      k_ogsp_gather<T, OP, MODE, 1, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
-                                                                 v, gv, a.grouped, a.perm);
+      k_ogsp_gather<T, OP, MODE, 1, 1><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, a.perm, nullptr);
     else
-      k_ogsp_gather<T, OP, MODE, 1, 0><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
-                                                                 v, gv, a.grouped, nullptr);
+      k_ogsp_gather<T, OP, MODE, 1, 0><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr, nullptr);
   } else if (kv == 4 && a.e2s) {
     k_ogso_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.colS, a.e2s, v, gv, a.grouped);
@@ -1131,12 +1180,18 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
     k_ogsa_gather<T, OP, MODE><<<persistent_grid(a.nchunks), kOgsThreads, 0, s>>>(
         a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped);
   } else if (kv >= 2) {
-    if (perm)
-      k_ogsp_gather<T, OP, MODE, 0, 1><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
-                                                                 v, gv, a.grouped, a.perm);
+    // the single-member path serves the in-place gather+scatter (MODE 0): there it
+    // saves the staging and the unchanged stores; a gather still writes every row,
+    // and measured slower with it
+    if (MODE == 0 && a.sing && a.grouped && tune(kTuneOgsSingles) == 1)
+      k_ogsp_gather<T, OP, 0, 0, 0, 1><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr, a.sing);
+    else if (perm)
+      k_ogsp_gather<T, OP, MODE, 0, 1><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, a.perm, nullptr);
     else
-      k_ogsp_gather<T, OP, MODE, 0, 0><<<pg, kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs, a.ids,
-                                                                 v, gv, a.grouped, nullptr);
+      k_ogsp_gather<T, OP, MODE, 0, 0><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr, nullptr);
   } else if (MODE == 0) {
     k_ogsw_gs_sym<T, OP><<<warp_grid(a.nchunks), kOgsThreads, 0, s>>>(a.chunks, a.nchunks, a.rs,
                                                                      a.ids, v, a.grouped);
@@ -1380,6 +1435,9 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->nchunksGS = p->gs_grouped = 0;
   if (p->d_waitErr) cudaFree(p->d_waitErr);
   p->d_waitErr = nullptr;
+  if (p->d_singT) cudaFree(p->d_singT);
+  if (p->d_singGS) cudaFree(p->d_singGS);
+  p->d_singT = p->d_singGS = nullptr;
   p->d_colIdsST = nullptr;
   p->d_rowOfST = p->d_e2sT = nullptr;
   int32_t* ptrs[] = {p->d_rowStartsT, p->d_colIdsT, p->d_blocksT};
@@ -1412,6 +1470,29 @@ static sp_status upload(const std::vector<E>& h, E** d, cudaStream_t s) {
 // need not share the walk that suits the gathers (measured on the permuted 64^3
 // p=7 box: gathers fastest on breadth-first pages of 512 entries, gather+scatter on
 // a renumbered walk of 256-entry pages in balls of 2^18 entries).
+// Per chunk (r0, r1, g0, g1): the number of its rows with more than one member and
+// their entries -- with rows grouped by size (largest first) those rows and
+// entries come first, the single-member rows after them.
+static std::vector<int32_t> singleton_split(const std::vector<int32_t>& quads,
+                                            const int32_t* rs) {
+  const int64_t nchunks = (int64_t)quads.size() / 4;
+  std::vector<int32_t> out(2 * std::max<int64_t>(nchunks, 1), 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < nchunks; ++c) {
+    int32_t k0 = 0, s0 = 0;
+    for (int32_t r = quads[4 * c]; r < quads[4 * c + 1]; ++r) {
+      const int32_t n = rs[r + 1] - rs[r];
+      if (n > 1) {
+        ++k0;
+        s0 += n;
+      }
+    }
+    out[2 * c] = k0;
+    out[2 * c + 1] = s0;
+  }
+  return out;
+}
+
 static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
   const int order = (int)tune(kTuneOgsGsOrder);
   if (order < 0 || p->nchunksT == 0) return SP_SUCCESS;
@@ -1449,6 +1530,7 @@ static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(rowsG, &p->d_rsGS, s))) return st;
     if ((st = upload(colIdsG, &p->d_ciGS, s))) return st;
     p->gs_grouped = 1;
+    if ((st = upload(singleton_split(quads, wrs), &p->d_singGS, s))) return st;
   } else if (order == 2) {
     if ((st = upload(walkRs, &p->d_rsGS, s))) return st;
     if ((st = upload(walkCi, &p->d_ciGS, s))) return st;
@@ -1625,6 +1707,7 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     if (tune(kTuneOgsRows) == 1 && p->nchunksT > 0) {
       build_grouped(chunksT, p->NrowsT, wrs, wci, rowsG, colIdsG);
       if ((st = upload(rowsG, &p->d_rowsGT, s))) return st;
+      if ((st = upload(singleton_split(chunksT, wrs), &p->d_singT, s))) return st;
       if ((st = upload(colIdsG, &p->d_colIdsGT, s))) return st;
       p->row_order = 1;
     }

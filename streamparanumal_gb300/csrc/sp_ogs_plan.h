@@ -161,6 +161,10 @@ struct sp_ogs_plan {
   int32_t gs_grouped = 0;
   int32_t* d_rsGS = nullptr;         // grouped rows, or the walk's row starts
   int32_t* d_ciGS = nullptr;         // grouped or walk column ids
+  // per chunk (rows with more than one member, their entries) of the grouped main
+  // walk and of the grouped gather+scatter walk (kernel 2's single-member path)
+  int32_t* d_singT = nullptr;
+  int32_t* d_singGS = nullptr;
   // count of bounded device waits that gave up (the bulk-staged gathers' waits)
   int32_t* d_waitErr = nullptr;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations

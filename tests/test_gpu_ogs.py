@@ -505,3 +505,88 @@ def test_bulk_staged_gathers_large_groups(cuda, orc):
     finally:
         for n, v in saved.items():
             capi.tune_set(n, v)
+
+
+SINGLE_KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
+                "ogs.page_shift", "ogs.ball_shift", "ogs.singles")
+
+
+@pytest.mark.parametrize("knobs", [
+    {"ogs.order": 0}, {"ogs.order": 1}, {"ogs.order": 2, "ogs.page_shift": 6},
+    {"ogs.order": 1, "ogs.ball_shift": 12, "ogs.gs_order": 2},
+    {"ogs.order": 1, "ogs.gs_order": 1, "ogs.gs_page_shift": 6}])
+@pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0),
+                                 (3, 3, 3, 15, 4)])
+def test_single_member_rows_path(cuda, orc, knobs, box):
+    """Kernel 2 with ogs.singles = 1: rows of one member bypass the staging; the
+    gather, the N-operator gather and the gather+scatter keep the reference's bits
+    for every op, including values whose first step changes them (-0 under Add,
+    -Inf and NaN under Max and Min)."""
+    saved = {n: capi.tune_get(n) for n in SINGLE_KNOBS + ("ogs.gs_page_shift",)}
+    try:
+        capi.tune_set("ogs.kernel", 2)
+        capi.tune_set("ogs.kernel.gather", 2)
+        capi.tune_set("ogs.rows", 1)
+        capi.tune_set("ogs.singles", 1)
+        for n, v in knobs.items():
+            capi.tune_set(n, v)
+        nx, ny, nz, p, seed = box
+        ids = O.box_hex_ids(nx, ny, nz, p, seed)
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        q = orc.uniform(ids.size, 81)
+        q[::11] = -0.0
+        q[::53] = -np.inf
+        q[::59] = np.nan
+        q[::61] = np.inf
+        gq = torch.zeros(rs.size - 1, dtype=torch.float64, device="cuda")
+        for op in (O.Add, O.Max, O.Min):
+            # equal values (NaN where the oracle has NaN) and equal signs of zeros
+            h.Gather(gq, torch.from_numpy(q).cuda(), 1, op, O.Trans)
+            got, want = host(gq), orc.gather(rs, ci, q, 1, op)
+            np.testing.assert_array_equal(got, want)
+            ok = ~np.isnan(want)  # a NaN made from Inf - Inf has no portable sign
+            np.testing.assert_array_equal(np.signbit(got[ok]), np.signbit(want[ok]))
+            dq = torch.from_numpy(q).cuda()
+            h.GatherScatter(dq, 1, op, O.Sym)
+            got, want = host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op)
+            np.testing.assert_array_equal(got, want, err_msg=f"op {op}")
+            ok = ~np.isnan(want)
+            np.testing.assert_array_equal(np.signbit(got[ok]), np.signbit(want[ok]))
+        qf = orc.uniform(ids.size, 82)
+        gN = torch.zeros(ref["rsN"].size - 1, dtype=torch.float64, device="cuda")
+        h.Gather(gN, torch.from_numpy(qf).cuda(), 1, O.Add, O.NoTrans)
+        np.testing.assert_array_equal(host(gN), orc.gather(ref["rsN"], ref["ciN"], qf))
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
+@pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
+def test_single_member_rows_path_types(cuda, orc, dtype, op):
+    saved = {n: capi.tune_get(n) for n in SINGLE_KNOBS}
+    try:
+        capi.tune_set("ogs.kernel", 2)
+        capi.tune_set("ogs.kernel.gather", 2)
+        capi.tune_set("ogs.rows", 1)
+        capi.tune_set("ogs.singles", 1)
+        ids = O.box_hex_ids(4, 3, 5, 3, 77)
+        h, ref = make(orc, ids)
+        rs, ci = ref["rsT"], ref["ciT"]
+        rng = np.random.default_rng(9)
+        if dtype == torch.float32:
+            q = rng.uniform(-1, 1, ids.size).astype(np.float32)
+            q[::37] = -0.0
+            q[::41] = -np.inf
+        else:
+            q = rng.integers(-9, 10, ids.size).astype(np.int32 if dtype == torch.int32 else np.int64)
+        gq = torch.zeros(rs.size - 1, dtype=dtype, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, op, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q, 1, op))
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, op, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q, 1, op))
+    finally:
+        for n, v in saved.items():
+            capi.tune_set(n, v)
