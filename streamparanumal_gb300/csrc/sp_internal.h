@@ -64,10 +64,12 @@ int64_t tune(TuneKey k);
 
 // ---------------------------------------------------------------- scratch layout
 // Layout of the caller-provided scratch of the single-launch reductions:
-//   [0, 8)                 : unsigned int ticket counter (+4 bytes pad)
-//   [256, 256 + 16*kMaxRedBlocks) : per-block partials (two doubles per block)
+//   [0, 8)                          : unsigned int ticket counter (+4 bytes pad)
+//   [256, 256 + 32*kMaxRedBlocks)   : per-block partials, 32 bytes per block (two
+//                                     doubles, or the integer-pipe accumulator)
 constexpr int    kMaxRedBlocks   = 2048;
 constexpr size_t kRedPartialOff  = 256;
-constexpr size_t kRedScratchSize = kRedPartialOff + 16 * (size_t)kMaxRedBlocks;
+constexpr size_t kRedPartialBytes = 32;
+constexpr size_t kRedScratchSize = kRedPartialOff + kRedPartialBytes * (size_t)kMaxRedBlocks;
 
 }  // namespace sp

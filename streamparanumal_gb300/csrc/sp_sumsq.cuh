@@ -17,10 +17,11 @@
 //     elements more than kWin binades below Emax, subnormals, Inf and NaN are
 //     added to an FP64 side sum with fma() -- FP64 semantics for the special
 //     values, negligible weight for the rest;
-//   * the lanes of a warp are combined as integers (aligned to the warp's largest
-//     window top, then 128-bit adds), so only one lane per warp converts to a
-//     double-double -- on GB300 the FP64 pipe is too narrow to let every lane do
-//     it; warps and blocks are combined in double-double in a fixed order.
+//   * lanes, warps and blocks are combined as integers (aligned to the larger
+//     window top, then 128-bit adds) in a fixed order, and the total becomes a
+//     double once, at the end -- on GB300 a dependent FP64 operation costs a
+//     whole warp slot of a 2-lane pipe, so a double-double tree over lanes or
+//     blocks would cost microseconds per launch.
 //
 // The result is the sum of squares to about 2^-59 relative (each term's error
 // is below that, and all terms are non-negative), i.e. it is within a few units
@@ -217,15 +218,17 @@ SP_SQ_HD DD dd_add(DD a, DD b) {
 }
 
 // The accumulator's value (plus the side sum) as a double-double: the four 32-bit
-// words are exact doubles, added in double-double (any 128-bit value).
-SP_SQ_HD DD value(const Acc& s) {
+// words are exact doubles, added in double-double (any 128-bit value).  `extra`
+// bits were shifted out of the words after accumulation (their unit is then
+// 2^extra times the accumulator's).
+SP_SQ_HD DD value(const Acc& s, int extra = 0) {
   DD v{0.0, 0.0};
   if (s.a0 | s.a1 | s.a2 | s.a3) {
     v = dd_add(DD{(double)s.a3 * 0x1p96, 0.0}, DD{(double)s.a2 * 0x1p64, 0.0});
     v = dd_add(v, DD{(double)s.a1 * 0x1p32, 0.0});
     v = dd_add(v, DD{(double)s.a0, 0.0});
     // unit of the accumulator: 2^(2 Emax - 2138), Emax >= 16
-    const int k = 2 * (int)(s.e20 >> 20) - 2138;
+    const int k = 2 * (int)(s.e20 >> 20) - 2138 + extra;
     v = DD{ldexp(v.hi, k), ldexp(v.lo, k)};
   }
   return dd_add(v, DD{s.f, 0.0});

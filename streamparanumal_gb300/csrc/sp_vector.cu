@@ -483,7 +483,7 @@ constexpr int kRedThreads = 256;
 
 struct RedScratch {
   unsigned int* ticket;
-  double* partial;  // 2*kMaxRedBlocks doubles
+  double* partial;  // kRedPartialBytes per block (two doubles, or an AccBits)
 };
 
 __host__ __device__ inline RedScratch red_scratch(void* p) {
@@ -628,17 +628,49 @@ k_dot_f32_fast(int64_t nvec, const float4* __restrict__ a, const float4* __restr
 // partials, an exact sum of zeros) returns out[0] unchanged.
 
 
-__device__ __forceinline__ sumsq::DD dd_shfl_down(sumsq::DD v, int h) {
-  return sumsq::DD{__shfl_down_sync(0xffffffffu, v.hi, h),
-                   __shfl_down_sync(0xffffffffu, v.lo, h)};
+// A block's (or a lane's) integer-pipe accumulator in 32 bytes of scratch or
+// shared memory: the four words, the window top, and the FP64 side sum.
+struct AccBits {
+  uint32_t a0, a1, a2, a3, e20, pad;
+  double f;
+};
+static_assert(sizeof(AccBits) == kRedPartialBytes, "one scratch slot per block");
+
+__device__ __forceinline__ void store_acc(AccBits* d, const sumsq::Acc& a) {
+  d->a0 = a.a0;
+  d->a1 = a.a1;
+  d->a2 = a.a2;
+  d->a3 = a.a3;
+  d->e20 = a.e20;
+  d->f = a.f;
+}
+// From shared memory (plain loads).
+__device__ __forceinline__ sumsq::Acc load_acc_shared(const AccBits* d) {
+  sumsq::Acc a;
+  a.a0 = d->a0;
+  a.a1 = d->a1;
+  a.a2 = d->a2;
+  a.a3 = d->a3;
+  a.e20 = d->e20;
+  a.f = d->f;
+  return a;
+}
+// From the global scratch written by other blocks (loads that bypass L1; these
+// are global-space loads and must never be given a shared-memory address).
+__device__ __forceinline__ sumsq::Acc load_acc_global(const AccBits* d) {
+  sumsq::Acc a;
+  a.a0 = __ldcg(&d->a0);
+  a.a1 = __ldcg(&d->a1);
+  a.a2 = __ldcg(&d->a2);
+  a.a3 = __ldcg(&d->a3);
+  a.e20 = __ldcg(&d->e20);
+  a.f = __ldcg(&d->f);
+  return a;
 }
 
-// The block's sum of squares as a double-double (valid in thread 0): each warp
-// adds its lanes' accumulators as integers (aligned to the warp's largest window
-// top) and the FP64 side sums in FP64, lane 0 converts once, and thread 0 adds
-// the warps' values in warp order.
-__device__ __forceinline__ sumsq::DD block_value(sumsq::Acc acc, sumsq::DD* s) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// The lanes' accumulators of a warp summed into lane 0: aligned to the warp's
+// largest window top, then 128-bit adds down a shuffle tree; side sums in FP64.
+__device__ __forceinline__ void warp_merge(sumsq::Acc& acc) {
   sumsq::align_to(acc, __reduce_max_sync(0xffffffffu, acc.e20));
 #pragma unroll
   for (int h = 16; h >= 1; h >>= 1) {
@@ -652,41 +684,35 @@ __device__ __forceinline__ sumsq::DD block_value(sumsq::Acc acc, sumsq::DD* s) {
 #pragma unroll
     for (int h = 16; h >= 1; h >>= 1) acc.f += __shfl_down_sync(0xffffffffu, acc.f, h);
   }
-  if (lane == 0) s[w] = sumsq::value(acc);
-  __syncthreads();
-  sumsq::DD r{0.0, 0.0};
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = sumsq::dd_add(r, s[i]);
-  __syncthreads();
-  return r;
 }
 
-// Double-double sum of v over the block, fixed order (valid in thread 0).
-__device__ __forceinline__ sumsq::DD block_sum_dd(sumsq::DD v, sumsq::DD* s) {
+// The block's sum as one accumulator (valid in thread 0): warps merge in
+// integers, thread 0 merges the warps' sums in warp order.
+__device__ __forceinline__ sumsq::Acc block_merge(sumsq::Acc acc, AccBits* sm) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int h = 16; h >= 1; h >>= 1) v = sumsq::dd_add(v, dd_shfl_down(v, h));
-  if (lane == 0) s[w] = v;
+  warp_merge(acc);
+  if (lane == 0) store_acc(sm + w, acc);
   __syncthreads();
-  sumsq::DD r{0.0, 0.0};
-  if (w == 0) {
-    r = (lane < (int)(blockDim.x >> 5)) ? s[lane] : sumsq::DD{0.0, 0.0};
-#pragma unroll
-    for (int h = 16; h >= 1; h >>= 1) r = sumsq::dd_add(r, dd_shfl_down(r, h));
-  }
+  if (threadIdx.x == 0)
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) sumsq::merge(acc, load_acc_shared(sm + i));
   __syncthreads();
-  return r;
+  return acc;
 }
 
-// Writes the block's double-double, and lets the last block to arrive add the
-// block values in block order (lane t takes blocks t, t + 256, ..., then the fixed
-// tree) into out[0]; out[1 .. nzero) = 0.
-__device__ __forceinline__ void finish_ticket_dd(sumsq::DD bv, RedScratch sc, double* out,
-                                                 sumsq::DD* s, int nzero) {
+// Bits the block partials drop when the last block sums them: the grid's total
+// then fits 128 bits for up to 2^41 elements.
+constexpr int kGridShift = 8;
+
+// Writes the block's accumulator (from thread 0), and lets the last block to arrive
+// sum the block partials in integers -- lane t takes blocks t, t + 256, ..., then
+// the warps and the block as above -- and round the total once into out[0];
+// out[1 .. nzero) = 0.
+__device__ __forceinline__ void finish_ticket_acc(const sumsq::Acc& bacc, RedScratch sc,
+                                                  double* out, AccBits* sm, int nzero) {
   __shared__ bool last;
+  AccBits* part = reinterpret_cast<AccBits*>(sc.partial);
   if (threadIdx.x == 0) {
-    sc.partial[2 * blockIdx.x] = bv.hi;
-    sc.partial[2 * blockIdx.x + 1] = bv.lo;
+    store_acc(part + blockIdx.x, bacc);
     __threadfence();
     const unsigned t = atomicAdd(sc.ticket, 1u);
     last = (t == gridDim.x - 1);
@@ -694,24 +720,27 @@ __device__ __forceinline__ void finish_ticket_dd(sumsq::DD bv, RedScratch sc, do
   __syncthreads();
   if (!last) return;
   __threadfence();
-  sumsq::DD v{0.0, 0.0};
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
-    v = sumsq::dd_add(v, sumsq::DD{__ldcg(sc.partial + 2 * i), __ldcg(sc.partial + 2 * i + 1)});
-  const sumsq::DD r = block_sum_dd(v, s);
+  sumsq::Acc a;
+  sumsq::init(a);
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    sumsq::Acc b = load_acc_global(part + i);
+    sumsq::shift_down(b, kGridShift);
+    sumsq::merge(a, b);
+  }
+  a = block_merge(a, sm);
   if (threadIdx.x == 0) {
+    const sumsq::DD r = sumsq::value(a, kGridShift);
     out[0] = r.hi + r.lo;
     *sc.ticket = 0u;  // leave the scratch zeroed for the next call
   }
   for (int i = 1 + threadIdx.x; i < nzero; i += blockDim.x) out[i] = 0.0;
 }
 
-// ROLL = true: the next U vectors of a lane are loaded while the current ones are
-// added (twice the registers for loads, loads always in flight).
 template <int U, int CTAS, bool ROLL>
 __global__ void __launch_bounds__(kRedThreads, CTAS)
 k_norm2_int(int64_t nvec, const double2* __restrict__ a, const double* __restrict__ as, int64_t n,
             void* scratch, double* out, int nzero) {
-  __shared__ sumsq::DD s[kRedThreads / 32];
+  __shared__ AccBits s[kRedThreads / 32];
   const RedScratch sc = red_scratch(scratch);
   sumsq::Acc acc;
   sumsq::init(acc);
@@ -754,7 +783,7 @@ k_norm2_int(int64_t nvec, const double2* __restrict__ a, const double* __restric
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) sumsq::add(acc, as[n - 1]);
-  finish_ticket_dd(block_value(acc, s), sc, out, s, nzero);
+  finish_ticket_acc(block_merge(acc, s), sc, out, s, nzero);
 }
 
 // Resident CTAs per SM (knob reduce.norm_ctas: 4 or 6; the kernel fits 6 x 256
@@ -840,7 +869,7 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
          double2* __restrict__ x, double2* __restrict__ r, const double* __restrict__ ps,
          const double* __restrict__ Aps, double* __restrict__ xs, double* __restrict__ rs,
          int64_t n, void* scratch, double* out) {
-  __shared__ sumsq::DD s[kRedThreads / 32];
+  __shared__ AccBits s[kRedThreads / 32];
   const RedScratch sc = red_scratch(scratch);
   sumsq::Acc acc;
   sumsq::init(acc);
@@ -887,7 +916,7 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
     rs[t] = nr;
     sumsq::add(acc, nr);
   }
-  finish_ticket_dd(block_value(acc, s), sc, out, s, 1);
+  finish_ticket_acc(block_merge(acc, s), sc, out, s, 1);
 }
 
 // FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
