@@ -85,12 +85,13 @@ void        sp_launch_count_reset(void);
  *    the column-major scatter (one thread per local column), 6 (gathers only) the
  *    pipelined gathers with each chunk's column ids staged in shared memory by TMA
  *    bulk copy one chunk ahead; defaults 2, 2, 5;
- *  "ogs.singles" (1 = the in-place gather+scatter through kernel 2 on rows
- *    grouped by size lets the rows of a single member skip the shared-memory
- *    staging and the combine loop: the lane that gathered such a value applies
- *    the op's first step and stores it back only when that changed its bits
- *    (-0 under Add, -Inf or NaN under Max/Min), so memory ends the same and
- *    unchanged values are not rewritten; default 1);
+ *  "ogs.singles" (0..2, default 2; kernel 2 on rows grouped by size: 1 = the
+ *    in-place gather+scatter lets the rows of a single member skip the
+ *    shared-memory staging and the combine loop -- the lane that gathered such a
+ *    value applies the op's first step and stores it back only when that changed
+ *    its bits (-0 under Add, -Inf or NaN under Max/Min), so memory ends the same
+ *    and unchanged values are not rewritten; 2 = as 1, and the gathers write
+ *    single-member rows from the gathering lane too);
  *  "ogs.scatter_pages" (1 = the column-major scatter takes the pages of local
  *    columns in the main walk's order when the plan has one (chunk orders 1 and 2)
  *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1);

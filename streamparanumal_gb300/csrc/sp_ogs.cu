@@ -465,15 +465,16 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
 #pragma unroll
     for (int u = 0; u < kOgsPerLane; ++u)
       if (lane + 32 * u < gn) val[u] = v[col[u]];
-    if (SG) {
+    if (SG && MODE == 0) {  // the single-member rows' words are not needed
       for (int32_t r = lane; r < k0; r += 32) {
         const int32_t wd = __ldg(rs + d.x + r);
         srs[r] = wd & 0xFFFF;
         sro[r] = (uint8_t)(wd >> 16);
       }
       if (lane == 0) srs[k0] = s0;
-    } else {
+    } else {  // a gather stages every row's word; SG then stops the combine at k0
       stage_rows(rs, grouped, d, lane, srs, sro);
+      if (SG && lane == 0) srs[k0] = s0;
     }
     int32_t coln[kOgsPerLane];
     load_cols(ids, dn, lane, coln);
@@ -482,14 +483,9 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
       const int32_t e = lane + 32 * u;
       if (e < s0) {
         sv[e] = val[u];
-      } else if (SG && e < gn) {
+      } else if (SG && MODE == 0 && e < gn) {
         const T y = Op<T, OP>::first(val[u]);
-        if (MODE == 1) {
-          const int32_t wd = __ldg(rs + d.x + k0 + (e - s0));
-          gv[op_row<PERM>(perm, d.x + (wd >> 16))] = y;
-        } else if (!same_bits(y, val[u])) {
-          v[col[u]] = y;
-        }
+        if (!same_bits(y, val[u])) v[col[u]] = y;
       }
     }
     if (PF) {
@@ -499,6 +495,14 @@ k_ogsp_gather(const int4* __restrict__ chunks, int32_t nchunks, const int32_t* _
         if (lane + 32 * u < gnn) prefetch_elem_l2(v + coln[u]);
     }
     __syncwarp();
+    if (SG && MODE == 1) {  // single-member rows: written from the gathering lane
+#pragma unroll
+      for (int u = 0; u < kOgsPerLane; ++u) {
+        const int32_t e = lane + 32 * u;
+        if (e >= s0 && e < gn)
+          gv[op_row<PERM>(perm, d.x + (int32_t)sro[k0 + (e - s0)])] = Op<T, OP>::first(val[u]);
+      }
+    }
     for (int32_t r = lane; r < k0; r += 32) {
       const RowRef q = staged_row(srs, sro, grouped, r);
       T acc = row_combine<T, OP>(sv, q.a, q.b);
@@ -1183,8 +1187,15 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
     // the single-member path serves the in-place gather+scatter (MODE 0): there it
     // saves the staging and the unchanged stores; a gather still writes every row,
     // and measured slower with it
-    if (MODE == 0 && a.sing && a.grouped && tune(kTuneOgsSingles) == 1)
+    const int64_t sgk = tune(kTuneOgsSingles);
+    if (MODE == 0 && a.sing && a.grouped && sgk >= 1)
       k_ogsp_gather<T, OP, 0, 0, 0, 1><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr, a.sing);
+    else if (MODE == 1 && a.sing && a.grouped && sgk == 2 && perm)
+      k_ogsp_gather<T, OP, 1, 0, 1, 1><<<pg, kOgsThreads, 0, s>>>(
+          a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, a.perm, a.sing);
+    else if (MODE == 1 && a.sing && a.grouped && sgk == 2)
+      k_ogsp_gather<T, OP, 1, 0, 0, 1><<<pg, kOgsThreads, 0, s>>>(
           a.chunks, a.nchunks, a.rs, a.ids, v, gv, a.grouped, nullptr, a.sing);
     else if (perm)
       k_ogsp_gather<T, OP, MODE, 0, 1><<<pg, kOgsThreads, 0, s>>>(

@@ -49,7 +49,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"reduce.norm_exact", 0, 1, {0}},
     {"reduce.norm_ctas", 4, 6, {4}},
     {"reduce.norm_roll", 0, 1, {1}},
-    {"ogs.singles", 0, 1, {1}},
+    {"ogs.singles", 0, 2, {2}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -114,7 +114,7 @@ KNOB_RANGES = {  # key: (lowest, highest, default), as include/sp_capi.h documen
     "ogs.kernel": (0, 6, 2), "ogs.kernel.gather": (0, 6, 2), "ogs.kernel.scatter": (0, 5, 5),
     "ogs.scatter_pages": (0, 1, 1), "reduce.norm_exact": (0, 1, 0),
     "reduce.norm_ctas": (4, 6, 4), "reduce.norm_roll": (0, 1, 1),
-    "ogs.singles": (0, 1, 1)}
+    "ogs.singles": (0, 2, 2)}
 
 
 @pytest.mark.parametrize("key", sorted(KNOB_RANGES))

@@ -517,7 +517,8 @@ SINGLE_KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs
     {"ogs.order": 1, "ogs.gs_order": 1, "ogs.gs_page_shift": 6}])
 @pytest.mark.parametrize("box", [(5, 4, 3, 7, 2024), (6, 6, 6, 2, 5), (7, 3, 2, 1, 0),
                                  (3, 3, 3, 15, 4)])
-def test_single_member_rows_path(cuda, orc, knobs, box):
+@pytest.mark.parametrize("singles", [1, 2])
+def test_single_member_rows_path(cuda, orc, knobs, box, singles):
     """Kernel 2 with ogs.singles = 1: rows of one member bypass the staging; the
     gather, the N-operator gather and the gather+scatter keep the reference's bits
     for every op, including values whose first step changes them (-0 under Add,
@@ -527,7 +528,7 @@ def test_single_member_rows_path(cuda, orc, knobs, box):
         capi.tune_set("ogs.kernel", 2)
         capi.tune_set("ogs.kernel.gather", 2)
         capi.tune_set("ogs.rows", 1)
-        capi.tune_set("ogs.singles", 1)
+        capi.tune_set("ogs.singles", singles)
         for n, v in knobs.items():
             capi.tune_set(n, v)
         nx, ny, nz, p, seed = box
@@ -564,13 +565,14 @@ def test_single_member_rows_path(cuda, orc, knobs, box):
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.int32, torch.int64])
 @pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
-def test_single_member_rows_path_types(cuda, orc, dtype, op):
+@pytest.mark.parametrize("singles", [1, 2])
+def test_single_member_rows_path_types(cuda, orc, dtype, op, singles):
     saved = {n: capi.tune_get(n) for n in SINGLE_KNOBS}
     try:
         capi.tune_set("ogs.kernel", 2)
         capi.tune_set("ogs.kernel.gather", 2)
         capi.tune_set("ogs.rows", 1)
-        capi.tune_set("ogs.singles", 1)
+        capi.tune_set("ogs.singles", singles)
         ids = O.box_hex_ids(4, 3, 5, 3, 77)
         h, ref = make(orc, ids)
         rs, ci = ref["rsT"], ref["ciT"]
