@@ -32,7 +32,8 @@ def test_status_strings(lib):
     assert lib.sp_status_string(capi.SP_ERR_CSR) == b"malformed CSR or ids"
     assert lib.sp_version() == 100
     assert lib.sp_ogs_block_nnz() == 2048
-    assert lib.sp_reduce_scratch_bytes() >= 256 + 16 * 1024
+    # a 256-byte header and 32 bytes for each of up to 2048 blocks
+    assert lib.sp_reduce_scratch_bytes() == 256 + 32 * 2048
 
 
 @pytest.mark.parametrize("fn,args", [
@@ -43,6 +44,9 @@ def test_status_strings(lib):
     ("sp_bs3_1_f64", (256, 257, 10, None, None, None)),      # nblocks > bs
     ("sp_reduce_finish_f64", (1024, 2000, None, None, None)),
     ("sp_norm2_f64", (10, None, None, None, None)),          # null scratch
+    ("sp_bs3_1_fast_f64", (100, 1, 10, None, None, None, None)),  # bad block size
+    ("sp_bs3_1_fast_f64", (256, 0, 10, None, None, None, None)),  # nblocks < 1
+    ("sp_bs3_1_fast_f64", (256, 4, 10, None, None, None, None)),  # null vector/scratch
     ("sp_ogs_gather_scatter", (None, 1, 0, 0, 1, None, None)),  # null plan
     ("sp_ogs_gather", (None, 1, 0, 0, 1, None, None, None)),
     ("sp_ogs_scatter", (None, 1, 0, 1, None, None, None)),
