@@ -84,7 +84,18 @@ void        sp_launch_count_reset(void);
  *    column-order scatter with L2 prefetch, 5 pipelined gathers with L2 prefetch or
  *    the column-major scatter (one thread per local column), 6 (gathers only) the
  *    pipelined gathers with each chunk's column ids staged in shared memory by TMA
- *    bulk copy one chunk ahead; defaults 2, 2, 5;
+ *    bulk copy one chunk ahead, 7 (gather and gather+scatter) lane-row slabs: each
+ *    lane combines whole rows in registers, rows of one size side by side, from the
+ *    plan's slab layout (no shared memory); defaults 2, 2, 5;
+ *  "ogs.slabs" (1 = plans created afterwards also hold the slab layouts kernel 7
+ *    runs on, about 4 bytes per entry and per row of each walk; default 0: kernel
+ *    7 then runs as kernel 2), "ogs.slab_seg_shift" (8..22, default 17: rows are
+ *    regrouped by size inside runs of 2^n entries of the walk);
+ *  "ogs.slab_lane" (0..16, default 0: members in flight per lane and pass of
+ *    kernel 7 -- 0 = 8 for 8-byte values and 16 for 4-byte ones, 1..8 = 8,
+ *    9..16 = 16) and "ogs.slab_ctas" (0..4, default 0: resident CTAs of 256
+ *    lanes per SM kernel 7 is compiled and launched for; 0 = 2), both for the
+ *    Add op (other ops run the defaults);
  *  "ogs.singles" (0..2, default 2; kernel 2 on rows grouped by size: 1 = the
  *    in-place gather+scatter lets the rows of a single member skip the
  *    shared-memory staging and the combine loop -- the lane that gathered such a
@@ -265,6 +276,8 @@ typedef struct {
   int32_t waitErrors; /* bounded device waits of this plan's kernels that gave up
                          (kernel 6's staging waits; 0 in every correct run; reading it
                          synchronises the device)                                  */
+  int32_t NslabsT;    /* lane-row slabs of the main walk (kernel 7; 0: not built)   */
+  int32_t NslabsGS;   /* lane-row slabs of the gather+scatter walk (0: none)         */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

@@ -3,7 +3,7 @@
 For a hex box of degree p it times BS6 (Gather Trans), BS7 (Scatter NoTrans) and
 BS8 (GatherScatter Sym) under every compiled variant -- block kernels (rows cut into
 blocks of `ogs.block_nnz` entries), warp-chunk kernels, pipelined persistent
-warp-chunk kernels and asynchronously staged ones, each with chunks in row order or
+warp-chunk kernels, asynchronously staged ones and lane-row slabs, each with chunks in row order or
 breadth-first page order (whole-mesh wavefronts or chains of balls) and rows in CSR
 order or grouped by size -- and keeps the fastest by total time.  The in-place
 gather+scatter then gets its own walk of the operator when one of the candidate
@@ -60,7 +60,12 @@ def gs_walks(p: int) -> list[dict]:
 KERNELS = {0: "block", 1: "warp", 2: "warp-pipelined",
            3: "warp-async-staged gathers / column-order scatter",
            4: "column-order gathers / persistent prefetching column-order scatter",
-           5: "pipelined gathers with L2 prefetch of the next chunk / column-major scatter"}
+           5: "pipelined gathers with L2 prefetch of the next chunk / column-major scatter",
+           7: "lane-row slabs (gather and gather+scatter)"}
+# lane-row slabs (kernel 7) regroup the walk's rows by size inside runs of 2^17
+# entries: on the 64^3 p = 7 box 2^16..2^18 measured within 2 % of each other, 2^14
+# 9 % and 2^19 and above 30 % slower
+SLAB_SEG_SHIFT = 17
 OPS = (("BS6", "kernel_gather"), ("BS7", "kernel_scatter"), ("BS8", "kernel_gs"))
 
 
@@ -82,10 +87,12 @@ KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift
          "gs_order": "ogs.gs_order", "gs_page_shift": "ogs.gs_page_shift",
          "gs_ball_shift": "ogs.gs_ball_shift",
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
-         "kernel_scatter": "ogs.kernel.scatter", "scatter_pages": "ogs.scatter_pages"}
+         "kernel_scatter": "ogs.kernel.scatter", "scatter_pages": "ogs.scatter_pages",
+         "slabs": "ogs.slabs", "slab_seg_shift": "ogs.slab_seg_shift"}
 # knobs a table entry may leave out: the library defaults
-PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1, "scatter_pages": 1}
-GS_WALK_KERNELS = (1, 2, 3, 5)
+PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1, "scatter_pages": 1, "slabs": 0,
+                 "slab_seg_shift": SLAB_SEG_SHIFT}
+GS_WALK_KERNELS = (1, 2, 3, 5, 7)
 
 
 def _set(cfg: dict) -> None:
@@ -107,8 +114,18 @@ def _kernels(pc: dict, op: str) -> list[int]:
             walked = pc["order"] >= 1 and pc["rows"] == 1
             ks += [1, 2] + ([3, 4] if pc["rows"] == 1 else []) + ([5] if plain or walked else [])
         else:
-            ks += [1, 2, 3, 4, 5]
+            ks += [1, 2, 3, 4, 5, 7]
     return ks
+
+
+def _slabs(choice: dict) -> dict:
+    """A chosen configuration builds the slab layouts only when a kernel 7 uses them."""
+    if 7 in (choice.get("kernel_gather"), choice.get("kernel_gs")):
+        choice.update(slabs=1, slab_seg_shift=SLAB_SEG_SHIFT)
+    else:
+        choice.pop("slabs", None)
+        choice.pop("slab_seg_shift", None)
+    return choice
 
 
 def choose(timings: list[tuple]) -> tuple[dict, float, float]:
@@ -143,7 +160,7 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
         if best_key is None or (main, gs_ms) < best_key:
             best_key, best, best_gs_ms = (main, gs_ms), choice, gs_ms
     best.setdefault("block_nnz", 2048)
-    return best, best_key[0], best_gs_ms
+    return _slabs(best), best_key[0], best_gs_ms
 
 
 def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int = 5,
@@ -166,7 +183,7 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
         return h
 
     try:
-        _set(PLAN_DEFAULTS)
+        _set({**PLAN_DEFAULTS, "slabs": 1})
         for pc in plan_configs(p):
             _set(pc)
             h = build()
@@ -202,6 +219,7 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
             if ms < best_gs_ms:
                 best.update(gs_order=go, gs_page_shift=gp, gs_ball_shift=gb, kernel_gs=k)
                 best_total += ms - best_gs_ms
+        _slabs(best)
     finally:
         _set(saved)
     return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,

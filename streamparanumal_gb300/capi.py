@@ -49,7 +49,8 @@ class OgsInfo(ctypes.Structure):
                 ("maxRowSize", c_int32), ("NgatherGlobal", c_int64), ("NchunksT", c_int32),
                 ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32),
                 ("NchunksGS", c_int32), ("gsRowOrder", c_int32), ("NpagesT", c_int32),
-                ("pageShift", c_int32), ("waitErrors", c_int32)]
+                ("pageShift", c_int32), ("waitErrors", c_int32), ("NslabsT", c_int32),
+                ("NslabsGS", c_int32)]
 
 
 class MrInfo(ctypes.Structure):

@@ -42,7 +42,7 @@ int sm_count();
 enum TuneKey : int {
   kTuneReducePrefetch = 0,  // order-exact reductions: L2 prefetch distance in chunks (-1 = per kernel)
   kTuneOgsBlockNnz,         // ogs plan: non-zeros per row block (256 .. 2048), read at plan creation
-  kTuneOgsKernel,           // ogs gather+scatter: 0 block, 1 warp-chunk, 2 pipelined, 3 async-staged (k == 1)
+  kTuneOgsKernel,           // ogs gather+scatter: 0 block, 1 warp-chunk, 2 pipelined, 3 async-staged, ..., 7 lane-row slabs (k == 1)
   kTuneOgsOrder,            // ogs plan: warp-chunk order, 0 = rows, 1 = breadth-first pages
   kTuneReduceRolling,       // order-exact reductions: 1 = rolling load pipeline, 0 = grouped
   kTuneOgsKernelGather,     // ogs gather: kernel variant as kTuneOgsKernel
@@ -58,6 +58,10 @@ enum TuneKey : int {
   kTuneNormCtas,            // integer-pipe norm: resident CTAs per SM (4 or 6)
   kTuneNormRoll,            // integer-pipe norm: 1 = rolling load pipeline
   kTuneOgsSingles,          // ogs kernel 2: 1 = single-member rows skip staging and combine
+  kTuneOgsSlabs,            // ogs plan: 1 = build the lane-row slab layouts (kernel 7)
+  kTuneOgsSlabSegShift,     // ogs plan: log2 of the entries regrouped together into slabs
+  kTuneOgsSlabLane,         // kernel 7: members in flight per lane (0 per type, 8 or 16)
+  kTuneOgsSlabCtas,         // kernel 7: resident CTAs per SM (0 = 2, 1..4)
   kTuneCount
 };
 int64_t tune(TuneKey k);

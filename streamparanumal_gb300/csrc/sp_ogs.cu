@@ -17,88 +17,11 @@
 #include <type_traits>
 #include <vector>
 
+#include "sp_ogs_ops.cuh"
 #include "sp_ogs_plan.h"
+#include "sp_ogs_slab.h"
 
 namespace sp {
-
-// ------------------------------------------------------------------ ops
-// Identities and update rules of libs/ogs/ogsUtils.cpp:62-103 (device) and
-// libs/ogs/ogsOperator.cpp:37-56 (host): Max/Min start from -+numeric max and
-// keep the current value unless the new one compares strictly greater/less.
-template <typename T> struct Lim;
-template <> struct Lim<float>  { static __device__ float big()  { return 3.402823466e+38f; } };
-template <> struct Lim<double> { static __device__ double big() { return 1.7976931348623157e+308; } };
-template <> struct Lim<int32_t> { static __device__ int32_t big() { return 2147483647; } };
-template <> struct Lim<long long> { static __device__ long long big() { return 9223372036854775807LL; } };
-
-template <typename T> __device__ __forceinline__ T wrap_add(T a, T b) { return a + b; }
-template <typename T> __device__ __forceinline__ T wrap_mul(T a, T b) { return a * b; }
-template <> __device__ __forceinline__ int32_t wrap_add(int32_t a, int32_t b) {
-  return (int32_t)((uint32_t)a + (uint32_t)b);
-}
-template <> __device__ __forceinline__ int32_t wrap_mul(int32_t a, int32_t b) {
-  return (int32_t)((uint32_t)a * (uint32_t)b);
-}
-template <> __device__ __forceinline__ long long wrap_add(long long a, long long b) {
-  return (long long)((unsigned long long)a + (unsigned long long)b);
-}
-template <> __device__ __forceinline__ long long wrap_mul(long long a, long long b) {
-  return (long long)((unsigned long long)a * (unsigned long long)b);
-}
-
-// first(v) is apply(init(), v) computed without floating-point arithmetic where
-// that is exact: identity + v == v for every v except -0 (which becomes +0), and
-// 1 * v == v.  On GB300 the FP64 pipe is narrow, and this removes one FP64 add per
-// row -- every add of a multiplicity-1 row -- without changing a single bit.
-__device__ __forceinline__ double plus_zero(double v) {
-  const long long b = __double_as_longlong(v);
-  return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
-}
-__device__ __forceinline__ float plus_zero(float v) {
-  const int b = __float_as_int(v);
-  return __int_as_float(b == (int)0x80000000u ? 0 : b);
-}
-__device__ __forceinline__ int32_t plus_zero(int32_t v) { return v; }
-__device__ __forceinline__ long long plus_zero(long long v) { return v; }
-
-template <typename T, int OP> struct Op;
-template <typename T> struct Op<T, SP_OP_ADD> {
-  static __device__ __forceinline__ T init() { return T(0); }
-  static __device__ __forceinline__ T first(T v) { return plus_zero(v); }
-  static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_add(a, b); }
-};
-template <typename T> struct Op<T, SP_OP_MUL> {
-  static __device__ __forceinline__ T init() { return T(1); }
-  static __device__ __forceinline__ T first(T v) { return v; }
-  static __device__ __forceinline__ void apply(T& a, T b) { a = wrap_mul(a, b); }
-};
-template <typename T> struct Op<T, SP_OP_MAX> {
-  static __device__ __forceinline__ T init() { return -Lim<T>::big(); }
-  static __device__ __forceinline__ T first(T v) {
-    T a = init();
-    apply(a, v);
-    return a;
-  }
-  static __device__ __forceinline__ void apply(T& a, T b) { a = (b > a) ? b : a; }
-};
-template <typename T> struct Op<T, SP_OP_MIN> {
-  static __device__ __forceinline__ T init() { return Lim<T>::big(); }
-  static __device__ __forceinline__ T first(T v) {
-    T a = init();
-    apply(a, v);
-    return a;
-  }
-  static __device__ __forceinline__ void apply(T& a, T b) { a = (b < a) ? b : a; }
-};
-
-// Combines s[a, b) in order from the op's identity.
-template <typename T, int OP>
-__device__ __forceinline__ T row_combine(const T* s, int32_t a, int32_t b) {
-  if (a >= b) return Op<T, OP>::init();
-  T acc = Op<T, OP>::first(s[a]);
-  for (int32_t i = a + 1; i < b; ++i) Op<T, OP>::apply(acc, s[i]);
-  return acc;
-}
 
 // ------------------------------------------------------------------ kernels
 
@@ -413,15 +336,6 @@ __device__ __forceinline__ void prefetch_elem_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
-// Bit equality (x = first(x) for most values: then a gather+scatter need not store).
-__device__ __forceinline__ bool same_bits(double a, double b) {
-  return __double_as_longlong(a) == __double_as_longlong(b);
-}
-__device__ __forceinline__ bool same_bits(float a, float b) {
-  return __float_as_int(a) == __float_as_int(b);
-}
-__device__ __forceinline__ bool same_bits(int32_t a, int32_t b) { return a == b; }
-__device__ __forceinline__ bool same_bits(long long a, long long b) { return a == b; }
 
 // PF = 1 (kernel 5): as soon as this chunk's values have landed, the next chunk's
 // values are prefetched into L2 from the column ids already in registers, so
@@ -1023,6 +937,10 @@ struct ChunkArgs {
   const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
   int32_t* waitErr;      // the plan's count of bounded waits that gave up
   const int2* sing;      // per chunk (multi-member rows, their entries), grouped rows only
+  const int4* slabs;     // lane-row slabs of the same walk (kernel 7), else null
+  int32_t nslabs;
+  const int32_t* slabIds;
+  const int32_t* slabRows;
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
@@ -1031,7 +949,9 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksT), p->nchunksT,
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
                    p->d_colIdsST, p->d_e2sT, p->d_permT, p->d_waitErr,
-                   g ? reinterpret_cast<const int2*>(p->d_singT) : nullptr};
+                   g ? reinterpret_cast<const int2*>(p->d_singT) : nullptr,
+                   reinterpret_cast<const int4*>(p->d_slabsT), p->nslabsT, p->d_slabIdsT,
+                   p->d_slabRowsT};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -1040,11 +960,14 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   const int32_t* ci = p->d_ciGS ? p->d_ciGS : p->d_colIdsT;
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
                    p->gs_grouped, nullptr, nullptr, nullptr, p->d_waitErr,
-                   p->gs_grouped ? reinterpret_cast<const int2*>(p->d_singGS) : nullptr};
+                   p->gs_grouped ? reinterpret_cast<const int2*>(p->d_singGS) : nullptr,
+                   reinterpret_cast<const int4*>(p->d_slabsGS), p->nslabsGS, p->d_slabIdsGS,
+                   nullptr};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
-                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr, nullptr};
+                   p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr, nullptr,
+                   nullptr, 0, nullptr, nullptr};
 }
 
 // Kernel 6: the pipelined persistent gathers of kernel 2 with the chunks' column ids
@@ -1167,8 +1090,11 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
   const bool perm = MODE == 1 && a.perm;
   if (perm && (kv == 3 || kv == 4)) kv = 2;
   if (kv == 6 && !a.waitErr) kv = 2;  // a plan without chunks has no wait-error word
+  if (kv == 7 && !a.slabs) kv = 2;     // a plan built without slabs (ogs.slabs = 0)
   const unsigned pg = persistent_grid(a.nchunks, kOgsPersistentCtas);
-  if (kv == 6) {
+  if (kv == 7) {
+    launch_slabs<T, OP, MODE>(a.slabs, a.nslabs, a.slabIds, a.slabRows, v, gv, s);
+  } else if (kv == 6) {
     launch_bulk_gather<T, OP, MODE>(a, v, gv, perm, s);
   } else if (kv == 5) {
     if (perm)
@@ -1446,6 +1372,10 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->nchunksGS = p->gs_grouped = 0;
   if (p->d_waitErr) cudaFree(p->d_waitErr);
   p->d_waitErr = nullptr;
+  for (int32_t* q : {p->d_slabsT, p->d_slabIdsT, p->d_slabRowsT, p->d_slabsGS, p->d_slabIdsGS})
+    if (q) cudaFree(q);
+  p->d_slabsT = p->d_slabIdsT = p->d_slabRowsT = p->d_slabsGS = p->d_slabIdsGS = nullptr;
+  p->nslabsT = p->nslabsGS = 0;
   if (p->d_singT) cudaFree(p->d_singT);
   if (p->d_singGS) cudaFree(p->d_singGS);
   p->d_singT = p->d_singGS = nullptr;
@@ -1504,6 +1434,24 @@ static std::vector<int32_t> singleton_split(const std::vector<int32_t>& quads,
   return out;
 }
 
+// Slab layout of one walk (build_slabs), uploaded; `rows_out` null for a walk that
+// only serves the in-place gather+scatter.
+static sp_status build_slab_layout(const std::vector<int32_t>& quads, const int32_t* wrs,
+                                   const int32_t* wci, const int32_t* perm, bool with_rows,
+                                   int32_t** desc_out, int32_t** ids_out, int32_t** rows_out,
+                                   int32_t* nslabs, cudaStream_t s) {
+  std::vector<int32_t> desc, ids, rows;
+  build_slabs(quads, wrs, wci, perm, (int)tune(kTuneOgsSlabSegShift), with_rows, desc, ids,
+              rows);
+  sp_status st;
+  if ((st = upload(desc, desc_out, s))) return st;
+  if ((st = upload(ids, ids_out, s))) return st;
+  if (rows_out && (st = upload(rows, rows_out, s))) return st;
+  *nslabs = (int32_t)(desc.size() / 4);
+  SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+  return SP_SUCCESS;
+}
+
 static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
   const int order = (int)tune(kTuneOgsGsOrder);
   if (order < 0 || p->nchunksT == 0) return SP_SUCCESS;
@@ -1547,6 +1495,10 @@ static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
     if ((st = upload(walkCi, &p->d_ciGS, s))) return st;
   }
   p->nchunksGS = (int32_t)(quads.size() / 4);
+  if (tune(kTuneOgsSlabs) == 1 &&
+      (st = build_slab_layout(quads, wrs, wci, nullptr, false, &p->d_slabsGS, &p->d_slabIdsGS,
+                              nullptr, &p->nslabsGS, s)))
+    return st;
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
 }
@@ -1722,6 +1674,11 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
       if ((st = upload(colIdsG, &p->d_colIdsGT, s))) return st;
       p->row_order = 1;
     }
+    // lane-row slabs of the main walk (kernel 7)
+    if (tune(kTuneOgsSlabs) == 1 && p->nchunksT > 0 &&
+        (st = build_slab_layout(chunksT, wrs, wci, renumber ? perm.data() : nullptr, true,
+                                &p->d_slabsT, &p->d_slabIdsT, &p->d_slabRowsT, &p->nslabsT, s)))
+      return st;
     // T chunk entries in column order: the column-order scatter and gathers
     std::vector<int32_t> colS;
     std::vector<uint8_t> rowOf, e2s;
@@ -1837,6 +1794,8 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->gsRowOrder = p->gs_grouped;
   info->NpagesT = p->npagesT;
   info->pageShift = p->pages_shift;
+  info->NslabsT = p->nslabsT;
+  info->NslabsGS = p->nslabsGS;
   info->waitErrors = 0;
   if (p->d_waitErr) {
     int32_t* dev = p->d_waitErr;

@@ -400,4 +400,116 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
   }
 }
 
+// Rows of chunks [c0, c1) in their walk order, stably regrouped by member count,
+// largest first (rows without members last, and only when `with_empty`).
+static void segment_rows(const std::vector<int32_t>& quads, int64_t c0, int64_t c1,
+                         const int32_t* rs, bool with_empty, std::vector<int64_t>& key) {
+  key.clear();
+  for (int64_t c = c0; c < c1; ++c)
+    for (int32_t r = quads[4 * c]; r < quads[4 * c + 1]; ++r) {
+      const int64_t m = rs[r + 1] - rs[r];
+      if (m > 0 || with_empty) key.push_back(((int64_t)(kOgsMaxRowSize - m) << 32) | (uint32_t)r);
+    }
+  std::stable_sort(key.begin(), key.end(),
+                   [](int64_t a, int64_t b) { return (a >> 32) < (b >> 32); });
+}
+
+// Words a slab of `entries` ids occupies: rounded up to 16 bytes, so that every
+// slab, and every pass of whole row steps inside it, starts on a 16-byte boundary.
+static inline int64_t slab_span(int64_t entries) { return (entries + 3) & ~int64_t(3); }
+
+int32_t slab_rows_per_lane(int32_t m) {
+  if (m <= 0) return kSlabLaneEntries;
+  return m <= kSlabLaneEntries ? kSlabLaneEntries / m : 1;
+}
+
+void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
+                 const int32_t* perm, int seg_shift, bool with_rows, std::vector<int32_t>& desc,
+                 std::vector<int32_t>& ids, std::vector<int32_t>& rows) {
+  const int64_t nchunks = (int64_t)quads.size() / 4;
+  // segments: runs of consecutive chunks of the walk holding >= 2^seg_shift entries
+  std::vector<int64_t> seg{0};
+  int64_t acc = 0;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    acc += quads[4 * c + 3] - quads[4 * c + 2];
+    if (acc >= (int64_t(1) << seg_shift)) {
+      seg.push_back(c + 1);
+      acc = 0;
+    }
+  }
+  if (seg.back() != nchunks) seg.push_back(nchunks);
+  const int64_t nseg = (int64_t)seg.size() - 1;
+  // pass 1: slabs, entries and rows of every segment
+  std::vector<int64_t> nS(nseg + 1, 0), nE(nseg + 1, 0), nW(nseg + 1, 0);
+#pragma omp parallel
+  {
+    std::vector<int64_t> key;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t g = 0; g < nseg; ++g) {
+      segment_rows(quads, seg[g], seg[g + 1], rs, with_rows, key);
+      int64_t S = 0, E = 0;
+      for (size_t a = 0; a < key.size();) {
+        const int32_t m = kOgsMaxRowSize - (int32_t)(key[a] >> 32);
+        size_t b = a;
+        while (b < key.size() && (key[b] >> 32) == (key[a] >> 32)) ++b;
+        const int64_t cap = 32LL * slab_rows_per_lane(m);
+        for (int64_t k0 = (int64_t)a; k0 < (int64_t)b; k0 += cap) {
+          ++S;
+          E += slab_span(std::min<int64_t>(cap, (int64_t)b - k0) * m);
+        }
+        a = b;
+      }
+      nS[g + 1] = S;
+      nE[g + 1] = E;
+      nW[g + 1] = with_rows ? (int64_t)key.size() : 0;
+    }
+  }
+  for (int64_t g = 0; g < nseg; ++g) {
+    nS[g + 1] += nS[g];
+    nE[g + 1] += nE[g];
+    nW[g + 1] += nW[g];
+  }
+  desc.assign(4 * nS[nseg], 0);
+  ids.assign(nE[nseg], 0);
+  rows.assign(nW[nseg], 0);
+  // pass 2: fill
+#pragma omp parallel
+  {
+    std::vector<int64_t> key;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t g = 0; g < nseg; ++g) {
+      segment_rows(quads, seg[g], seg[g + 1], rs, with_rows, key);
+      int64_t S = nS[g], E = nE[g], Wr = nW[g];
+      for (size_t a = 0; a < key.size();) {
+        const int32_t m = kOgsMaxRowSize - (int32_t)(key[a] >> 32);
+        size_t b = a;
+        while (b < key.size() && (key[b] >> 32) == (key[a] >> 32)) ++b;
+        const int64_t cap = 32LL * slab_rows_per_lane(m);
+        for (size_t k0 = a; k0 < b; k0 += cap) {
+          const int32_t n = (int32_t)std::min<int64_t>(cap, (int64_t)(b - k0));
+          const int32_t nl = std::min(32, n);
+          const int32_t Re = (n + nl - 1) / nl;
+          const int32_t rem = n - (Re - 1) * nl;
+          desc[4 * S + 0] = (int32_t)E;
+          desc[4 * S + 1] = (int32_t)Wr;
+          desc[4 * S + 2] = m;
+          desc[4 * S + 3] = nl | (rem << 8) | (Re << 16);
+          for (int32_t k = 0; k < n; ++k) {
+            const int32_t j = k / nl, l = k % nl;
+            const int32_t w = (j == Re - 1) ? rem : nl;
+            const int32_t r = (int32_t)(uint32_t)key[k0 + k];
+            for (int32_t t = 0; t < m; ++t)
+              ids[E + (int64_t)j * m * nl + (int64_t)t * w + l] = ci[rs[r] + t];
+            if (with_rows) rows[Wr + k] = perm ? perm[r] : r;
+          }
+          E += slab_span((int64_t)n * m);
+          if (with_rows) Wr += n;
+          ++S;
+        }
+        a = b;
+      }
+    }
+  }
+}
+
 }  // namespace sp

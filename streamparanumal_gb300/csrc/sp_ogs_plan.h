@@ -86,6 +86,26 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
                   const int32_t* rowsG, const int32_t* colIdsE, std::vector<int32_t>& colIdsS,
                   std::vector<uint8_t>& rowOfS, std::vector<uint8_t>& e2s);
 
+// Lane-row slabs (kernel 7).  The rows of a walk (its chunks in visit order) are
+// cut into segments of about 2^seg_shift entries; inside a segment the rows are
+// regrouped by member count m (largest first, walk order kept within a size) and
+// cut into slabs of at most 32 * R rows of one size, R = slab_rows_per_lane(m)
+// rows per lane.  A slab of n rows uses nl = min(32, n) lanes and Re = ceil(n / nl)
+// row steps; step j holds rows j*nl + l (lane l < nl, the last step only rem =
+// n - (Re-1)*nl of them).  Member t of row (j, l) is ids[E + j*m*nl + t*w_j + l]
+// with w_j = nl (rem for the last step): member-major, so the lanes' t-th loads
+// are neighbouring words.  Each slab's ids start on a 16-byte boundary (up to 3
+// unused words follow a slab whose entry count is not a multiple of 4), so a run
+// of whole row steps can be copied in 16-byte pieces.  desc holds per slab (E, first
+// row word, m, nl | rem << 8 | Re << 16); rows[first + j*nl + l] is the operator
+// row of (j, l) (perm applied; only when `with_rows`, which also keeps the rows
+// without members, as slabs of m = 0).  Each row keeps its members in CSR order.
+constexpr int32_t kSlabLaneEntries = 16;
+int32_t slab_rows_per_lane(int32_t m);
+void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
+                 const int32_t* perm, int seg_shift, bool with_rows, std::vector<int32_t>& desc,
+                 std::vector<int32_t>& ids, std::vector<int32_t>& rows);
+
 // Element slots of an nx*ny*nz box: slot[e] is where lexicographic element e is
 // stored (identity for perm_seed 0, else a seeded Fisher-Yates shuffle).
 std::vector<int32_t> box_slots(int64_t E, uint64_t perm_seed);
@@ -165,6 +185,15 @@ struct sp_ogs_plan {
   // walk and of the grouped gather+scatter walk (kernel 2's single-member path)
   int32_t* d_singT = nullptr;
   int32_t* d_singGS = nullptr;
+  // lane-row slabs (kernel 7, knob ogs.slabs): of the main walk (descriptors, ids,
+  // operator rows) and of the gather+scatter walk when the plan has one (no rows)
+  int32_t* d_slabsT = nullptr;
+  int32_t* d_slabIdsT = nullptr;
+  int32_t* d_slabRowsT = nullptr;
+  int32_t nslabsT = 0;
+  int32_t* d_slabsGS = nullptr;
+  int32_t* d_slabIdsGS = nullptr;
+  int32_t nslabsGS = 0;
   // count of bounded device waits that gave up (the bulk-staged gathers' waits)
   int32_t* d_waitErr = nullptr;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations

@@ -1,0 +1,16 @@
+// Lane-row slab gathers (kernel 7): launch entry points used by the ogs dispatch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sp {
+
+// One launch over the slabs of a walk (build_slabs): MODE 1 gathers gv[row] = op
+// over the row's members of v (rows from `rows`); MODE 0 writes that result back
+// to every member of v in place (gather+scatter, Sym), `rows` unused.
+template <typename T, int OP, int MODE>
+void launch_slabs(const int4* slabs, int32_t nslabs, const int32_t* ids, const int32_t* rows,
+                  T* v, T* gv, cudaStream_t s);
+
+}  // namespace sp

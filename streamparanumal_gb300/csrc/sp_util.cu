@@ -34,10 +34,10 @@ struct TuneEntry {
 static TuneEntry g_tune[kTuneCount] = {
     {"reduce.prefetch_chunks", -1, 64, {-1}},
     {"ogs.block_nnz", 256, 2048, {2048}},
-    {"ogs.kernel", 0, 6, {2}},
+    {"ogs.kernel", 0, 7, {2}},
     {"ogs.order", 0, 2, {1}},
     {"reduce.rolling", 0, 1, {1}},
-    {"ogs.kernel.gather", 0, 6, {2}},
+    {"ogs.kernel.gather", 0, 7, {2}},
     {"ogs.kernel.scatter", 0, 5, {5}},
     {"ogs.rows", 0, 1, {1}},
     {"ogs.page_shift", 3, 16, {9}},
@@ -50,6 +50,10 @@ static TuneEntry g_tune[kTuneCount] = {
     {"reduce.norm_ctas", 4, 6, {4}},
     {"reduce.norm_roll", 0, 1, {1}},
     {"ogs.singles", 0, 2, {2}},
+    {"ogs.slabs", 0, 1, {0}},
+    {"ogs.slab_seg_shift", 8, 22, {17}},
+    {"ogs.slab_lane", 0, 16, {0}},
+    {"ogs.slab_ctas", 0, 4, {0}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

@@ -115,10 +115,11 @@ KNOB_RANGES = {  # key: (lowest, highest, default), as include/sp_capi.h documen
     "ogs.block_nnz": (256, 2048, 2048), "ogs.order": (0, 2, 1), "ogs.page_shift": (3, 16, 9),
     "ogs.rows": (0, 1, 1), "ogs.ball_shift": (0, 26, 0), "ogs.gs_order": (-1, 2, -1),
     "ogs.gs_page_shift": (3, 16, 8), "ogs.gs_ball_shift": (0, 26, 18),
-    "ogs.kernel": (0, 6, 2), "ogs.kernel.gather": (0, 6, 2), "ogs.kernel.scatter": (0, 5, 5),
+    "ogs.kernel": (0, 7, 2), "ogs.kernel.gather": (0, 7, 2), "ogs.kernel.scatter": (0, 5, 5),
     "ogs.scatter_pages": (0, 1, 1), "reduce.norm_exact": (0, 1, 0),
     "reduce.norm_ctas": (4, 6, 4), "reduce.norm_roll": (0, 1, 1),
-    "ogs.singles": (0, 2, 2)}
+    "ogs.singles": (0, 2, 2), "ogs.slabs": (0, 1, 0), "ogs.slab_seg_shift": (8, 22, 17),
+    "ogs.slab_lane": (0, 16, 0), "ogs.slab_ctas": (0, 4, 0)}
 
 
 @pytest.mark.parametrize("key", sorted(KNOB_RANGES))

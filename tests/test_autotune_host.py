@@ -35,10 +35,10 @@ def test_kernel_candidates():
     grouped = {"order": 1, "rows": 1, "block_nnz": 2048, "page_shift": 9}
     plain_rows = {"order": 0, "rows": 0, "block_nnz": 2048, "page_shift": 9}
     small_blocks = {"order": 0, "rows": 0, "block_nnz": 1024, "page_shift": 9}
-    assert autotune._kernels(grouped, "BS6") == [1, 2, 3, 4, 5]
+    assert autotune._kernels(grouped, "BS6") == [1, 2, 3, 4, 5, 7]
     assert autotune._kernels(grouped, "BS7") == [1, 2, 3, 4, 5]
     assert autotune._kernels(dict(grouped, rows=0), "BS7") == [1, 2]
-    assert autotune._kernels(plain_rows, "BS8") == [0, 1, 2, 3, 4, 5]
+    assert autotune._kernels(plain_rows, "BS8") == [0, 1, 2, 3, 4, 5, 7]
     assert autotune._kernels(plain_rows, "BS7") == [0, 1, 2, 5]
     assert autotune._kernels(small_blocks, "BS6") == [0]
 
@@ -61,7 +61,10 @@ def test_committed_table_is_well_formed():
     for key, cfg in table.items():
         assert key.startswith("p")
         assert set(cfg) <= set(autotune.KNOBS)
-        assert cfg["order"] in (0, 1, 2) and cfg["kernel_gs"] in range(6)
+        assert cfg["order"] in (0, 1, 2) and cfg["kernel_gs"] in (0, 1, 2, 3, 4, 5, 7)
+        # the slab layouts are built exactly where a kernel 7 runs on them
+        uses = 7 in (cfg["kernel_gather"], cfg["kernel_gs"])
+        assert cfg.get("slabs", 0) == int(uses)
 
 
 def test_text_form_matches_the_table():
@@ -115,3 +118,13 @@ def test_choose_block_kernels_keep_their_block_size():
                                            (0, 0, 9, 0, 2048, 5, "BS7"): 0.5}))
     assert best["kernel_gather"] == 0 and best["block_nnz"] == 1024
     assert best["kernel_scatter"] == 5 and best["scatter_pages"] == 0
+
+
+def test_choose_lane_row_slabs_builds_their_layout():
+    walk = (1, 1, 9, 19, 2048)
+    best, _, _ = autotune.choose(_timings({walk + (7, "BS6"): 0.5, walk + (5, "BS7"): 0.5,
+                                           walk + (2, "BS8"): 0.5}))
+    assert best["kernel_gather"] == 7 and best["kernel_gs"] == 2
+    assert best["slabs"] == 1 and best["slab_seg_shift"] == autotune.SLAB_SEG_SHIFT
+    best, _, _ = autotune.choose(_timings({walk + (2, "BS6"): 0.5, walk + (5, "BS7"): 0.5}))
+    assert 7 not in (best["kernel_gather"], best["kernel_gs"]) and "slabs" not in best
