@@ -18,12 +18,12 @@ def test_tune_and_apply_small_box(cuda, orc, tmp_path):
         assert set(best) >= {"order", "rows", "page_shift", "kernel_gs", "kernel_gather",
                              "kernel_scatter", "block_nnz"}
         # grouped plans (2, plus 64-entry pages at p = 3, plus the renumbered walk,
-        # plus the three breadth-first ones as chains of balls) x (5 + 4 + 5) kernels
+        # plus the three breadth-first ones as chains of balls) x (6 + 4 + 6) kernels
         # and the walk-ordered column-major scatter under the six breadth-first ones,
-        # the breadth-first CSR plan x (5 + 2 + 5), the row-order CSR plan with block
-        # kernels and the column-major scatter too (6 + 4 + 6), and block kernels at
+        # the breadth-first CSR plan x (6 + 2 + 6), the row-order CSR plan with block
+        # kernels and the column-major scatter too (7 + 4 + 7), and block kernels at
         # block_nnz 1024 (3); then the gather+scatter walks x their kernels
-        assert len(res["candidates"]) == 98 + 6 + 12 + 16 + 3
+        assert len(res["candidates"]) == 112 + 6 + 14 + 18 + 3
         assert len(res["gs_walks"]) in (0, len(autotune.GS_WALK_KERNELS) * len(autotune.gs_walks(3)))
         table = {}
         autotune.record(table, res)
