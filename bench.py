@@ -5,7 +5,8 @@ One step = one pass of the FP64 BS1-BS8 suite, each kernel called exactly as the
 reference's drivers call it:
   BS1 copy, BS2 axpy, BS3 norm (bs3_1+bs3_2; stage 1 is the integer-pipe norm that
   the drivers run by default), BS4 dot (bs4_1+bs4_2), BS5 CG update
-  (bs5_1+bs5_2) on vectors of N = 2^28 doubles (the top of the 2^10..2^28 sweep), and
+  (bs5_1+bs5_2; stage 1 with r.r on the integer pipe, the drivers' default) on
+  vectors of N = 2^28 doubles (the top of the 2^10..2^28 sweep), and
   BS6 gather, BS7 scatter, BS8 gather+scatter on a 64x64x64 hex box at p=7 whose
   element slots are permuted from a seed (134,217,728 local / 90,518,849 global nodes).
 value = sum of the reference's accounted bytes (bs{1..8}Run.cpp) / step time, GB/s.
@@ -361,8 +362,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         call("sp_bs4_1_f64", 256, nb256, N, a.data_ptr(), b.data_ptr(), tmp.data_ptr(), sptr)
         call("sp_reduce_finish_f64", 256, nb256, tmp.data_ptr(), scal.data_ptr() + 8, sptr)
         yield "BS4"
-        call("sp_bs5_1_f64", 1024, nb1024, N, a.data_ptr(), alpha, b.data_ptr(), tmp.data_ptr(),
-             sptr)
+        # the drivers' default BS5: r updated as the reference does, r.r on the integer
+        # pipe, the reference's stage 2
+        call("sp_bs5_1_fast_f64", 1024, nb1024, N, a.data_ptr(), alpha, b.data_ptr(),
+             tmp.data_ptr(), red.ptr, sptr)
         call("sp_reduce_finish_f64", 1024, nb1024, tmp.data_ptr(), scal.data_ptr() + 16, sptr)
         yield "BS5"
         h.Gather(gq, q, 1, O.Add, O.Trans, stream=stream)
@@ -649,7 +652,7 @@ def storage_forms(stream, dev, h_a, h_b, h_q, h, N, Nt, Ng, per, alpha, beta) ->
         form("CG", ms32, 24 * N, {"rdotr_rel_err_vs_fp64": abs(r[7] - r[6]) / abs(r[6]),
                                   "x_max_rel_err_vs_fp64": xerr})
         # the reference's BS5 update (r += alpha Ap, r.r) stored in FP32, one launch,
-        # against the order-exact FP64 BS5 of the suite
+        # against the FP64 BS5 of the suite
         f64["BS5"] = 24 * N
         r5, Ap5 = b.clone(), a.flip(0).contiguous()
         call("sp_cg_update_ref_f64", N, cg_alpha, Ap5.data_ptr(), r5.data_ptr(),

@@ -108,6 +108,8 @@ void        sp_launch_count_reset(void);
  *    and a page holds at least 1 KiB of values, 0 = in memory order; default 1);
  *  "reduce.norm_exact" (0 = the C++ platform's bs3_1 binding runs the integer-pipe
  *    norm sp_bs3_1_fast_f64, 1 = the order-exact sp_bs3_1_f64; default 0);
+ *  "reduce.rdotr_exact" (0 = the C++ platform's bs5_1 binding runs
+ *    sp_bs5_1_fast_f64, 1 = the order-exact sp_bs5_1_f64; default 0);
  *  "reduce.norm_ctas" (4 or 6, default 4): resident CTAs of 256 lanes per SM, and
  *    CTAs per SM of the persistent grid, of the integer-pipe norm (values 5 run 4);
  *  "reduce.norm_roll" (1 = the integer-pipe norm keeps the next loads of each lane
@@ -218,6 +220,18 @@ sp_status sp_norm2_f64(int64_t n, const double* a, double* out, void* scratch, s
  * order-exact sp_bs3_1_f64 stays available (knob "reduce.norm_exact"). */
 sp_status sp_bs3_1_fast_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* a,
                             double* partial, void* scratch, sp_stream_t stream);
+/* Stage 1 of BS5 in the same form, for the call sites of bs5_1 (BS/BS5/src/bs5Run.cpp:87):
+ * r = fma(alpha, Ap, r) as sp_bs5_1_f64 stores it (the same bits), partial[0] = sum r*r
+ * over the stored r on the integer pipe (as sp_norm2_f64: within a few ulps of the
+ * exactly rounded sum, hence within 1e-14 relative of the reference's order-exact
+ * bs5_1/bs5_2, BS/BS5/okl/bs5.okl:27-106) and partial[1 .. nblocks) = 0, so that the
+ * unchanged stage 2 returns partial[0].  One FP64 fma per entry instead of two: the
+ * order-exact form is bound by GB300's FP64 pipe and HBM together.  The drivers'
+ * default; the order-exact sp_bs5_1_f64 stays available (knob "reduce.rdotr_exact").
+ * block_size and nblocks as for sp_bs5_1_f64; scratch as above. */
+sp_status sp_bs5_1_fast_f64(int32_t block_size, int32_t nblocks, int64_t n, const double* Ap,
+                            double alpha, double* r, double* partial, void* scratch,
+                            sp_stream_t stream);
 sp_status sp_dot_f64(int64_t n, const double* a, const double* b, double* out, void* scratch,
                      sp_stream_t stream);
 sp_status sp_norm2_f32(int64_t n, const float* a, double* out, void* scratch, sp_stream_t stream);

@@ -89,6 +89,8 @@ SIGNATURES = {
     "sp_bs2_axpy_f32": (c_int32, [c_int64, c_float, _P, c_float, _P, _P]),
     "sp_bs3_1_f64": (c_int32, [c_int32, c_int32, c_int64, _P, _P, _P]),
     "sp_bs3_1_fast_f64": (c_int32, [c_int32, c_int32, c_int64, _P, _P, _P, _P]),
+    "sp_bs5_1_fast_f64": (c_int32, [c_int32, c_int32, c_int64, _P, c_double, _P, _P, _P,
+                                    _P]),
     "sp_bs4_1_f64": (c_int32, [c_int32, c_int32, c_int64, _P, _P, _P, _P]),
     "sp_bs5_1_f64": (c_int32, [c_int32, c_int32, c_int64, _P, c_double, _P, _P, _P]),
     "sp_reduce_finish_f64": (c_int32, [c_int32, c_int32, _P, _P, _P]),

@@ -58,6 +58,7 @@ enum TuneKey : int {
   kTuneNormCtas,            // integer-pipe norm: resident CTAs per SM (4 or 6)
   kTuneNormRoll,            // integer-pipe norm: 1 = rolling load pipeline
   kTuneOgsSingles,          // ogs kernel 2: 1 = single-member rows skip staging and combine
+  kTuneRdotrExact,          // BS5 at the drivers' bs5_1 call sites: 0 integer-pipe r.r, 1 order-exact
   kTuneOgsSlabs,            // ogs plan: 1 = build the lane-row slab layouts (kernel 7)
   kTuneOgsSlabSegShift,     // ogs plan: log2 of the entries regrouped together into slabs
   kTuneOgsSlabLane,         // kernel 7: members in flight per lane (0 per type, 8 or 16)

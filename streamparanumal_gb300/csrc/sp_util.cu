@@ -50,6 +50,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"reduce.norm_ctas", 4, 6, {4}},
     {"reduce.norm_roll", 0, 1, {1}},
     {"ogs.singles", 0, 2, {2}},
+    {"reduce.rdotr_exact", 0, 1, {0}},
     {"ogs.slabs", 0, 1, {0}},
     {"ogs.slab_seg_shift", 8, 22, {17}},
     {"ogs.slab_lane", 0, 16, {0}},

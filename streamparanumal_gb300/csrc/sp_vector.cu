@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(kRedThreads)
 k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double2* __restrict__ Ap,
          double2* __restrict__ x, double2* __restrict__ r, const double* __restrict__ ps,
          const double* __restrict__ Aps, double* __restrict__ xs, double* __restrict__ rs,
-         int64_t n, void* scratch, double* out) {
+         int64_t n, void* scratch, double* out, int nzero) {
   __shared__ AccBits s[kRedThreads / 32];
   const RedScratch sc = red_scratch(scratch);
   sumsq::Acc acc;
@@ -916,7 +916,7 @@ k_cg_f64(int64_t nvec, double alpha, const double2* __restrict__ p, const double
     rs[t] = nr;
     sumsq::add(acc, nr);
   }
-  finish_ticket_acc(block_merge(acc, s), sc, out, s, 1);
+  finish_ticket_acc(block_merge(acc, s), sc, out, s, nzero);
 }
 
 // FP32 storage: x, r, p, Ap in FP32; update in FP32 with alpha rounded to FP32;
@@ -1169,7 +1169,7 @@ sp_status sp_cg_update_f64(int64_t n, double alpha, const double* p, const doubl
                 as_cuda(stream)>>>(
       nvec, alpha, reinterpret_cast<const double2*>(p), reinterpret_cast<const double2*>(Ap),
       reinterpret_cast<double2*>(x), reinterpret_cast<double2*>(r), p, Ap, x, r, n, scratch,
-      rdotr);
+      rdotr, 1);
   return check_launch("sp_cg_update_f64");
 }
 
@@ -1195,8 +1195,23 @@ sp_status sp_cg_update_ref_f64(int64_t n, double alpha, const double* Ap, double
   k_cg_f64<U, false><<<red_grid((const void*)k_cg_f64<U, false>, nvec, U), kRedThreads, 0,
                        as_cuda(stream)>>>(
       nvec, alpha, nullptr, reinterpret_cast<const double2*>(Ap), nullptr,
-      reinterpret_cast<double2*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr);
+      reinterpret_cast<double2*>(r), nullptr, Ap, nullptr, r, n, scratch, rdotr, 1);
   return check_launch("sp_cg_update_ref_f64");
+}
+
+sp_status sp_bs5_1_fast_f64(int32_t bs, int32_t nblocks, int64_t n, const double* Ap,
+                            double alpha, double* r, double* partial, void* scratch,
+                            sp_stream_t stream) {
+  sp_status st = check_exact_args(bs, nblocks, n, "sp_bs5_1_fast_f64");
+  if (st) return st;
+  if ((st = check_red_args(n, scratch, partial, {Ap, r}, "sp_bs5_1_fast_f64"))) return st;
+  constexpr int U = 2;
+  const int64_t nvec = n / 2;
+  k_cg_f64<U, false><<<red_grid((const void*)k_cg_f64<U, false>, nvec, U), kRedThreads, 0,
+                       as_cuda(stream)>>>(
+      nvec, alpha, nullptr, reinterpret_cast<const double2*>(Ap), nullptr,
+      reinterpret_cast<double2*>(r), nullptr, Ap, nullptr, r, n, scratch, partial, nblocks);
+  return check_launch("sp_bs5_1_fast_f64");
 }
 
 sp_status sp_cg_update_ref_f32(int64_t n, double alpha, const float* Ap, float* r,

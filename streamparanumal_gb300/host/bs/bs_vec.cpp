@@ -34,8 +34,8 @@ void bsVecSettings(settings_t& s) {
   s.newSetting("-cg", "--cg-full", "CG FULL", "FALSE",
                "BS5 as the full CG update x+=alpha p, r-=alpha Ap, r.r", {"TRUE", "FALSE"});
   s.newSetting("-ex", "--exact-norm", "EXACT NORM", "FALSE",
-               "BS3 in the reference's summation order (bit-identical; bound by the FP64 "
-               "pipe) instead of the integer-pipe norm", {"TRUE", "FALSE"});
+               "BS3 norm and BS5 r.r in the reference's summation order (bit-identical; "
+               "bound by the FP64 pipe) instead of on the integer pipe", {"TRUE", "FALSE"});
   s.newSetting("-v", "--verbose", "VERBOSE", "FALSE", "Enable verbose output", {"TRUE", "FALSE"});
 }
 
@@ -142,8 +142,8 @@ int nblock_for(size_t N, int blockSize) {
 void bsVecRun(int which, platform_t& platform, settings_t& settings) {
   const bool fp32 = settings.compareSetting("PRECISION", "FP32");
   const bool cgFull = (which == 5) && settings.compareSetting("CG FULL", "TRUE");
-  if (which == 3)
-    checkStatus(sp_tune_set("reduce.norm_exact",
+  if (which == 3 || which == 5)
+    checkStatus(sp_tune_set(which == 3 ? "reduce.norm_exact" : "reduce.rdotr_exact",
                             settings.compareSetting("EXACT NORM", "TRUE") ? 1 : 0),
                 "EXACT NORM");
   const size_t word = fp32 ? sizeof(float) : sizeof(dfloat);

@@ -118,11 +118,18 @@ sp_status k_bs4_1(const Args& a, int bs, cudaStream_t s) {
   return sp_bs4_1_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, (const double*)a[3].p,
                       (double*)a[4].p, (sp_stream_t)s);
 }
-// bs5.okl:27-67: (Nblocks, N, Ap, alpha, r, rdotr)
+// bs5.okl:27-67: (Nblocks, N, Ap, alpha, r, rdotr).  r updated as the reference
+// does; r.r on the integer pipe by default (rdotr[0], rdotr[1..Nblocks) = 0, so
+// bs5_2 returns it); the order-exact kernel under the knob reduce.rdotr_exact = 1.
 sp_status k_bs5_1(const Args& a, int bs, cudaStream_t s) {
   expect(a, "bs5_1", {I, I, P, R, P, P});
-  return sp_bs5_1_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, a[3].d,
-                      (double*)a[4].p, (double*)a[5].p, (sp_stream_t)s);
+  int64_t exact = 0;
+  if (sp_status st = sp_tune_get("reduce.rdotr_exact", &exact)) return st;
+  if (exact)
+    return sp_bs5_1_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, a[3].d,
+                        (double*)a[4].p, (double*)a[5].p, (sp_stream_t)s);
+  return sp_bs5_1_fast_f64(bs, (int32_t)a[0].i, a[1].i, (const double*)a[2].p, a[3].d,
+                           (double*)a[4].p, (double*)a[5].p, reduce_scratch(), (sp_stream_t)s);
 }
 // bs3_2 / bs4_2 / bs5_2 (identical): (Nblocks, a, out)
 sp_status k_finish(const Args& a, int bs, cudaStream_t s) {

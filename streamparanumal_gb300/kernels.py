@@ -114,6 +114,16 @@ def bs5_1(Nblocks: int, N: int, o_Ap, alpha: float, o_r, o_tmp, block_size: int 
               o_r.data_ptr(), o_tmp.data_ptr(), _stream(stream))
 
 
+def bs5_1_fast(Nblocks: int, N: int, o_Ap, alpha: float, o_r, o_tmp, scratch: "ReduceScratch",
+               block_size: int = 1024, stream=None) -> None:
+    """bs5_1 with r.r on the integer pipe (the drivers' default): r = r + alpha Ap as
+    bs5_1 stores it, o_tmp[0] = r.r, o_tmp[1:Nblocks] = 0, so bs5_2 returns o_tmp[0]."""
+    for t, n in ((o_Ap, "o_Ap"), (o_r, "o_r"), (o_tmp, "o_tmp")):
+        _chk(t, (torch.float64,), n)
+    capi.call("sp_bs5_1_fast_f64", block_size, Nblocks, N, o_Ap.data_ptr(), float(alpha),
+              o_r.data_ptr(), o_tmp.data_ptr(), scratch.ptr, _stream(stream))
+
+
 def reduce_finish(Nblocks: int, o_tmp, o_out, block_size: int = 256, stream=None) -> None:
     """bs3_2 / bs4_2 / bs5_2."""
     capi.call("sp_reduce_finish_f64", block_size, Nblocks, o_tmp.data_ptr(), o_out.data_ptr(),

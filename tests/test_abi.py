@@ -47,6 +47,9 @@ def test_status_strings(lib):
     ("sp_bs3_1_fast_f64", (100, 1, 10, None, None, None, None)),  # bad block size
     ("sp_bs3_1_fast_f64", (256, 0, 10, None, None, None, None)),  # nblocks < 1
     ("sp_bs3_1_fast_f64", (256, 4, 10, None, None, None, None)),  # null vector/scratch
+    ("sp_bs5_1_fast_f64", (100, 1, 10, None, 1.0, None, None, None, None)),  # bad block size
+    ("sp_bs5_1_fast_f64", (1024, 1025, 10, None, 1.0, None, None, None, None)),  # nblocks > bs
+    ("sp_bs5_1_fast_f64", (1024, 4, 10, None, 1.0, None, None, None, None)),  # null vectors
     ("sp_ogs_gather_scatter", (None, 1, 0, 0, 1, None, None)),  # null plan
     ("sp_ogs_gather", (None, 1, 0, 0, 1, None, None, None)),
     ("sp_ogs_scatter", (None, 1, 0, 1, None, None, None)),
@@ -118,7 +121,7 @@ KNOB_RANGES = {  # key: (lowest, highest, default), as include/sp_capi.h documen
     "ogs.kernel": (0, 7, 2), "ogs.kernel.gather": (0, 7, 2), "ogs.kernel.scatter": (0, 5, 5),
     "ogs.scatter_pages": (0, 1, 1), "reduce.norm_exact": (0, 1, 0),
     "reduce.norm_ctas": (4, 6, 4), "reduce.norm_roll": (0, 1, 1),
-    "ogs.singles": (0, 2, 2), "ogs.slabs": (0, 1, 0), "ogs.slab_seg_shift": (8, 22, 17),
+    "ogs.singles": (0, 2, 2), "reduce.rdotr_exact": (0, 1, 0), "ogs.slabs": (0, 1, 0), "ogs.slab_seg_shift": (8, 22, 17),
     "ogs.slab_lane": (0, 16, 0), "ogs.slab_ctas": (0, 4, 0)}
 
 

@@ -60,7 +60,7 @@ def test_bs0_rows(cuda, bsdir):
 @pytest.mark.parametrize("which,title", [(1, "Copy"), (2, "AXPY"), (3, "Norm"), (4, "Dot"),
                                          (5, "CG Update")])
 @pytest.mark.parametrize("extra", [[], ["-fp", "FP32"], ["-cg", "TRUE"],
-                                   ["-fp", "FP32", "-cg", "TRUE"]])
+                                   ["-fp", "FP32", "-cg", "TRUE"], ["-ex", "TRUE"]])
 def test_bs1_to_bs5_rows(cuda, bsdir, which, title, extra):
     out = run(bsdir, f"BS{which}", "-b", 1 << 22, *extra).stdout
     assert re.fullmatch(rf"BS{which} = \[{ROW_VEC}\]; %{title} \[DOFs, elapsed, DOFs/s, BW "

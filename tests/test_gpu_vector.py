@@ -187,6 +187,32 @@ def test_bs3_fast_norm(cuda, orc, n, kind):
     assert abs(got - ref) <= 1e-14 * ref
 
 
+@pytest.mark.parametrize("n", [1, 2, 1 << 10, (1 << 16) + 3, (1 << 22) + 1])
+@pytest.mark.parametrize("kind", ["uniform", "wide", "zeros", "subnormal"])
+@pytest.mark.parametrize("bs", [1024, 256])
+def test_bs5_fast_update(cuda, orc, n, kind, bs):
+    """The drivers' default BS5 (r update as the reference stores it, r.r on the
+    integer pipe, then the reference's stage 2): r bit for bit as the order-exact
+    bs5_1 (CUDA fma), r.r within 4 ulps of the double-double sum of the stored r and
+    within 1e-14 relative of the reference's order-exact result."""
+    Ap = norm_inputs(orc, n, kind)
+    r0 = orc.uniform(n, 77 + n)
+    alpha = 0.37
+    nb = K.nblocks_for(n, bs)
+    r = dev(r0)
+    tmp = torch.full((bs,), float("nan"), dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    K.bs5_1_fast(nb, n, dev(Ap), alpha, r, tmp, K.ReduceScratch(), block_size=bs)
+    K.reduce_finish(nb, tmp, out, block_size=bs)
+    want_r, _, ref = orc.bs5(Ap, alpha, r0, bs=bs, nblocks=nb, fmad=1)
+    np.testing.assert_array_equal(host(r), want_r)
+    assert np.all(host(tmp)[1:nb] == 0.0)
+    got = host(out)[0]
+    exact = orc.dot_dd(want_r, want_r)
+    assert abs(got - exact) <= 4 * np.spacing(exact)
+    assert abs(got - ref) <= 1e-14 * ref
+
+
 def test_bs3_fast_norm_special_values(cuda, orc):
     sc = K.ReduceScratch()
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
