@@ -193,7 +193,18 @@ __device__ __forceinline__ void slab_rest(const int32_t* __restrict__ ids,
 // the values of the current pass are in flight (one memory round trip per pass),
 // the next slab's descriptor one slab ahead.  Row words are loaded beside the
 // values they are stored with.
-template <typename T, int OP, int MODE, int KB, int CTAS>
+// Value load of a full pass: LD 0 plain (L1 and L2), 1 L2 only (ld.global.cg), 2
+// evict-first (ld.global.cs), 3 through the read-only path (ld.global.nc; gathers
+// only, whose v the kernel never writes).
+template <int LD, int MODE, typename T>
+__device__ __forceinline__ T load_val(const T* p) {
+  if constexpr (LD == 1) return __ldcg(p);
+  else if constexpr (LD == 2) return __ldcs(p);
+  else if constexpr (LD == 3 && MODE == 1) return __ldg(p);
+  else return *p;
+}
+
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0>
 __global__ void __launch_bounds__(kOgsThreads, CTAS)
 k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __restrict__ ids,
               const int32_t* __restrict__ rows, T* v, T* gv) {
@@ -225,7 +236,7 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
       T val[KB];
       int32_t rw[KB];
 #pragma unroll
-      for (int u = 0; u < KB; ++u) val[u] = v[cid[u]];
+      for (int u = 0; u < KB; ++u) val[u] = load_val<LD, MODE>(v + cid[u]);
       if (MODE == 1) {
         const int32_t* rsrc = rows + d.y + j0 * 32 + lane;
 #pragma unroll
@@ -266,13 +277,13 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
   }
 }
 
-template <typename T, int OP, int MODE, int KB, int CTAS>
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0>
 static void launch_shape(const int4* slabs, int32_t nslabs, const int32_t* ids,
                          const int32_t* rows, T* v, T* gv, cudaStream_t s) {
   const int64_t want = ((int64_t)nslabs + kWarpsPerCta - 1) / kWarpsPerCta;
   const int64_t cap = (int64_t)sm_count() * CTAS;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min(want, cap));
-  k_ogsl_gather<T, OP, MODE, KB, CTAS><<<g, kOgsThreads, 0, s>>>(slabs, nslabs, ids, rows, v,
+  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD><<<g, kOgsThreads, 0, s>>>(slabs, nslabs, ids, rows, v,
                                                                  gv);
 }
 
@@ -283,6 +294,12 @@ static void launch_ctas(const int4* slabs, int32_t nslabs, const int32_t* ids,
                         const int32_t* rows, T* v, T* gv, cudaStream_t s) {
   constexpr int dflt = SlabCtas<(int)sizeof(T), KB>::value;
   if constexpr (OP == SP_OP_ADD) {
+    switch (tune(kTuneOgsSlabLoad)) {
+      case 1: return launch_shape<T, OP, MODE, KB, dflt, 1>(slabs, nslabs, ids, rows, v, gv, s);
+      case 2: return launch_shape<T, OP, MODE, KB, dflt, 2>(slabs, nslabs, ids, rows, v, gv, s);
+      case 3: return launch_shape<T, OP, MODE, KB, dflt, 3>(slabs, nslabs, ids, rows, v, gv, s);
+      default: break;
+    }
     switch (tune(kTuneOgsSlabCtas)) {
       case 1: return launch_shape<T, OP, MODE, KB, 1>(slabs, nslabs, ids, rows, v, gv, s);
       case 3: return launch_shape<T, OP, MODE, KB, 3>(slabs, nslabs, ids, rows, v, gv, s);

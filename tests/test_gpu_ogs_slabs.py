@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 
 KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
          "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.slabs", "ogs.slab_seg_shift",
-         "ogs.slab_lane", "ogs.page_shift", "ogs.ball_shift")
+         "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.page_shift",
+         "ogs.ball_shift")
 
 
 @pytest.fixture
@@ -97,6 +98,31 @@ def test_slab_segments_and_kernel_shapes(cuda, orc, knobs, seg, lane):
     dq = torch.from_numpy(q.copy()).cuda()
     h.GatherScatter(dq, 1, O.Add, O.Sym)
     np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+
+
+@pytest.mark.parametrize("load", [1, 2, 3])
+@pytest.mark.parametrize("ctas", [1, 3, 4])
+def test_slab_load_paths_and_ctas(cuda, orc, knobs, load, ctas):
+    """The value-load variants (L2 only, evict-first, read-only path) and the
+    resident-CTA shapes of kernel 7 give the same bits, FP64 and FP32."""
+    knobs("ogs.order", 1)
+    knobs("ogs.slab_load", load)
+    ids = O.box_hex_ids(6, 5, 4, 7, 2024)
+    h, ref = make(orc, ids)
+    check_fp64(orc, h, ref, ids.size, 5)
+    knobs("ogs.slab_load", 0)
+    knobs("ogs.slab_ctas", ctas)
+    check_fp64(orc, h, ref, ids.size, 6)
+    rs, ci = ref["rsT"], ref["ciT"]
+    for lv in (load, 0):
+        knobs("ogs.slab_load", lv)
+        q = orc.uniform(ids.size, 10 + lv).astype(np.float32)
+        gq = torch.zeros(rs.size - 1, dtype=torch.float32, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64, torch.int32, torch.int64])
