@@ -92,9 +92,10 @@ void        sp_launch_count_reset(void);
  *    7 then runs as kernel 2), "ogs.slab_seg_shift" (8..22, default 17: rows are
  *    regrouped by size inside runs of 2^n entries of the walk);
  *  "ogs.slab_lane" (0..16, default 0: members in flight per lane and pass of
- *    kernel 7 -- 0 = 8 for 8-byte values and 16 for 4-byte ones, 1..8 = 8,
+ *    kernel 7 -- 0 = 8, and 16 for the gather+scatter of 4-byte values, 1..8 = 8,
  *    9..16 = 16), "ogs.slab_ctas" (0..4, default 0: resident CTAs of 256
- *    lanes per SM kernel 7 is compiled and launched for; 0 = 2) and
+ *    lanes per SM kernel 7 is compiled and launched for; 0 = 3 for 4-byte values
+ *    at 8 members per lane, else 2) and
  *    "ogs.slab_load" (0..3, default 0: kernel 7's value loads -- 0 plain, 1 L2
  *    only, 2 evict-first, 3 the read-only path for gathers, plain for the in-place
  *    gather+scatter; with the default CTAs), all for the Add op (other ops run the

@@ -29,10 +29,12 @@
 
 namespace sp {
 
-// Resident CTAs of 256 lanes per SM each kernel shape is compiled for by default.
+// Resident CTAs of 256 lanes per SM each kernel shape is compiled for by default:
+// 3 for 4-byte values at 8 members per lane, else 2 (the sweeps on GB300 of 1..4
+// CTAs per shape; more CTAs spill, or, without spills, lowered the DRAM rate).
 template <int BYTES, int KB>
 struct SlabCtas {
-  static constexpr int value = 2;
+  static constexpr int value = (BYTES == 4 && KB == 8) ? 3 : 2;
 };
 
 // Row steps [j0, j0 + P) of a slab of M-member rows (M, P known at compile time).
@@ -310,15 +312,16 @@ static void launch_ctas(const int4* slabs, int32_t nslabs, const int32_t* ids,
   launch_shape<T, OP, MODE, KB, dflt>(slabs, nslabs, ids, rows, v, gv, s);
 }
 
-// Members in flight per lane and pass: 8 for 8-byte values, 16 for 4-byte ones
-// (knob ogs.slab_lane 0); 8 or 16 for both when the knob says so.  The other
-// shape is compiled for Add, the op the benchmarks time; the other ops run the
-// default shape.
+// Members in flight per lane and pass: 8, except 16 for the in-place
+// gather+scatter of 4-byte values (knob ogs.slab_lane 0; measured on GB300: FP32
+// gathers 8 per lane at 3 CTAs per SM +10 % over 16 at 2, the FP32 gather+scatter
+// 16 at 2 +3 % over 8 at 3); 8 or 16 when the knob says so.  The other shape is
+// compiled for Add, the op the benchmarks time; the other ops run the default.
 template <typename T, int OP, int MODE>
 void launch_slabs(const int4* slabs, int32_t nslabs, const int32_t* ids, const int32_t* rows,
                   T* v, T* gv, cudaStream_t s) {
   if (nslabs <= 0) return;
-  constexpr int KB = sizeof(T) == 4 ? 16 : 8;
+  constexpr int KB = (sizeof(T) == 4 && MODE == 0) ? 16 : 8;
   constexpr int KO = KB == 16 ? 8 : 16;
   if constexpr (OP == SP_OP_ADD) {
     const int64_t lane = tune(kTuneOgsSlabLane);
