@@ -128,3 +128,16 @@ def test_choose_lane_row_slabs_builds_their_layout():
     assert best["slabs"] == 1 and best["slab_seg_shift"] == autotune.SLAB_SEG_SHIFT
     best, _, _ = autotune.choose(_timings({walk + (2, "BS6"): 0.5, walk + (5, "BS7"): 0.5}))
     assert 7 not in (best["kernel_gather"], best["kernel_gs"]) and "slabs" not in best
+
+
+def test_choose_counts_the_gather_scatter_time_of_each_layout():
+    # the plain layout is a little faster for BS6 + BS7 but its gather+scatter is
+    # slow; the grouped walk wins on the three together
+    walk, plain = (1, 1, 9, 19, 2048), (0, 0, 9, 0, 2048)
+    best, main, gs = autotune.choose(_timings({
+        plain + (7, "BS6"): 0.40, plain + (5, "BS7"): 0.40, plain + (1, "BS8"): 0.9,
+        walk + (7, "BS6"): 0.45, walk + (5, "BS7"): 0.45, walk + (2, "BS8"): 0.5}))
+    assert (best["order"], best["rows"], best["ball_shift"]) == (1, 1, 19)
+    # (BS7 takes the memory-order column-major scatter of the plain plan, which
+    # competes under every layout)
+    assert best["kernel_gs"] == 2 and abs(main - 0.85) < 1e-12 and gs == 0.5

@@ -121,3 +121,9 @@ def test_bs2_to_bs5_match_reference_values(cuda, orc, path):
             r_ser, _, _ = orc.bs5(ha, al, hb, bs=1024, fmad=0)
             assert sha(r_ser) == g["sha256"]["bs5_r"]
             assert close_to_serial(r.cpu().numpy(), r_ser, al * ha)
+        # the drivers' default stage 1 (r.r on the integer pipe): the same r
+        r2 = b.clone()
+        K.bs5_1_fast(nb5, n, a, al, r2, tmp, K.ReduceScratch(), block_size=bs)
+        K.bs5_2(nb5, tmp, out, block_size=bs)
+        assert torch.equal(r2, r)
+        assert abs(out.item() - val[key]) <= 1e-14 * val[key]
