@@ -64,6 +64,7 @@ enum TuneKey : int {
   kTuneOgsSlabLane,         // kernel 7: members in flight per lane (0 per type, 8 or 16)
   kTuneOgsSlabCtas,         // kernel 7: resident CTAs per SM (0 = 2, 1..4)
   kTuneOgsSlabLoad,         // kernel 7: value loads 0 plain, 1 L2 only, 2 evict-first, 3 read-only path
+  kTuneOgsSlabDefer,        // kernel 7 gather+scatter: 1 = a pass's stores after the next pass's loads
   kTuneCount
 };
 int64_t tune(TuneKey k);

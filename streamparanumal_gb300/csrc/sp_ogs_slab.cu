@@ -157,6 +157,38 @@ __device__ __forceinline__ void pass_combine(const T (&val)[KB], const int32_t (
   }
 }
 
+// The in-place gather+scatter's combine of a full pass with its stores deferred:
+// the results and their columns are kept (pval, pcid, mask pm) and stored after the
+// next pass's values have been requested.  Columns of different rows never
+// coincide, so the later loads cannot see these stores early or late.
+template <typename T, int OP, int M, int KB>
+__device__ __forceinline__ void pass_defer(const T (&val)[KB], const int32_t (&cid)[KB],
+                                           T (&pval)[KB], int32_t (&pcid)[KB], uint32_t& pm) {
+  constexpr int P = KB / M;
+#pragma unroll
+  for (int jj = 0; jj < P; ++jj) {
+    T acc = Op<T, OP>::first(val[jj * M]);
+#pragma unroll
+    for (int t = 1; t < M; ++t) Op<T, OP>::apply(acc, val[jj * M + t]);
+#pragma unroll
+    for (int t = 0; t < M; ++t) {
+      const int u = jj * M + t;
+      pval[u] = acc;
+      pcid[u] = cid[u];
+      if (M > 1 || !same_bits(acc, val[u])) pm |= 1u << u;
+    }
+  }
+}
+
+template <typename T, int KB>
+__device__ __forceinline__ void flush_deferred(T* v, const T (&pval)[KB],
+                                               const int32_t (&pcid)[KB], uint32_t& pm) {
+#pragma unroll
+  for (int u = 0; u < KB; ++u)
+    if (pm & (1u << u)) v[pcid[u]] = pval[u];
+  pm = 0u;
+}
+
 // The rest of a slab from step j0 (its last, partial step and any full steps that
 // do not fill a pass), or a whole slab of another row size.
 template <typename T, int OP, int MODE, int KB>
@@ -206,10 +238,16 @@ __device__ __forceinline__ T load_val(const T* p) {
   else return *p;
 }
 
-template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0>
+// DF = 1 (gather+scatter only): a full pass's stores are issued after the next
+// pass's value loads.
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
 __global__ void __launch_bounds__(kOgsThreads, CTAS)
 k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __restrict__ ids,
               const int32_t* __restrict__ rows, T* v, T* gv) {
+  constexpr bool defer = DF != 0 && MODE == 0;
+  T pval[KB];
+  int32_t pcid[KB];
+  uint32_t pm = 0u;
   const int lane = threadIdx.x & 31;
   const int32_t W = gridDim.x * kWarpsPerCta;
   int32_t s = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
@@ -250,13 +288,24 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
 #pragma unroll
         for (int u = 0; u < KB; ++u) nid[u] = __ldg(src + 32 * u);
       }
-      switch (m) {
-        case 1: pass_combine<T, OP, MODE, 1, KB>(val, cid, rw, v, gv); break;
-        case 2: pass_combine<T, OP, MODE, 2, KB>(val, cid, rw, v, gv); break;
-        case 4: pass_combine<T, OP, MODE, 4, KB>(val, cid, rw, v, gv); break;
-        default: pass_combine<T, OP, MODE, 8, KB>(val, cid, rw, v, gv);
+      if constexpr (defer) {
+        flush_deferred<T, KB>(v, pval, pcid, pm);
+        switch (m) {
+          case 1: pass_defer<T, OP, 1, KB>(val, cid, pval, pcid, pm); break;
+          case 2: pass_defer<T, OP, 2, KB>(val, cid, pval, pcid, pm); break;
+          case 4: pass_defer<T, OP, 4, KB>(val, cid, pval, pcid, pm); break;
+          default: pass_defer<T, OP, 8, KB>(val, cid, pval, pcid, pm);
+        }
+      } else {
+        switch (m) {
+          case 1: pass_combine<T, OP, MODE, 1, KB>(val, cid, rw, v, gv); break;
+          case 2: pass_combine<T, OP, MODE, 2, KB>(val, cid, rw, v, gv); break;
+          case 4: pass_combine<T, OP, MODE, 4, KB>(val, cid, rw, v, gv); break;
+          default: pass_combine<T, OP, MODE, 8, KB>(val, cid, rw, v, gv);
+        }
       }
     } else {
+      if constexpr (defer) flush_deferred<T, KB>(v, pval, pcid, pm);
       slab_rest<T, OP, MODE, KB>(ids, rows, v, gv, d, j0, lane);
       if (fullx) {
         const int32_t* src = ids + dx.x + jx * dx.z * 32 + lane;
@@ -277,16 +326,17 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
       for (int u = 0; u < KB; ++u) cid[u] = nid[u];
     }
   }
+  if constexpr (defer) flush_deferred<T, KB>(v, pval, pcid, pm);
 }
 
-template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0>
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
 static void launch_shape(const int4* slabs, int32_t nslabs, const int32_t* ids,
                          const int32_t* rows, T* v, T* gv, cudaStream_t s) {
   const int64_t want = ((int64_t)nslabs + kWarpsPerCta - 1) / kWarpsPerCta;
   const int64_t cap = (int64_t)sm_count() * CTAS;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min(want, cap));
-  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD><<<g, kOgsThreads, 0, s>>>(slabs, nslabs, ids, rows, v,
-                                                                 gv);
+  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD, DF><<<g, kOgsThreads, 0, s>>>(slabs, nslabs, ids, rows,
+                                                                     v, gv);
 }
 
 // One pass size with the resident CTAs the knob ogs.slab_ctas asks for (Add only;
@@ -295,6 +345,10 @@ template <typename T, int OP, int MODE, int KB>
 static void launch_ctas(const int4* slabs, int32_t nslabs, const int32_t* ids,
                         const int32_t* rows, T* v, T* gv, cudaStream_t s) {
   constexpr int dflt = SlabCtas<(int)sizeof(T), KB>::value;
+  if constexpr (OP == SP_OP_ADD && MODE == 0) {
+    if (tune(kTuneOgsSlabDefer) == 1)
+      return launch_shape<T, OP, MODE, KB, dflt, 0, 1>(slabs, nslabs, ids, rows, v, gv, s);
+  }
   if constexpr (OP == SP_OP_ADD) {
     switch (tune(kTuneOgsSlabLoad)) {
       case 1: return launch_shape<T, OP, MODE, KB, dflt, 1>(slabs, nslabs, ids, rows, v, gv, s);

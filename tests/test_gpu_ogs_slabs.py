@@ -16,8 +16,8 @@ pytestmark = pytest.mark.gpu
 
 KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
          "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.slabs", "ogs.slab_seg_shift",
-         "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.page_shift",
-         "ogs.ball_shift")
+         "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.slab_defer",
+         "ogs.page_shift", "ogs.ball_shift")
 
 
 @pytest.fixture
@@ -123,6 +123,29 @@ def test_slab_load_paths_and_ctas(cuda, orc, knobs, load, ctas):
         dq = torch.from_numpy(q.copy()).cuda()
         h.GatherScatter(dq, 1, O.Add, O.Sym)
         np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+
+
+@pytest.mark.parametrize("seg", [8, 17])
+@pytest.mark.parametrize("lane", [0, 16])
+def test_slab_deferred_stores(cuda, orc, knobs, seg, lane):
+    """The gather+scatter with each pass's stores issued after the next pass's
+    loads (ogs.slab_defer): the same bits, FP64 and FP32, with -0 made +0."""
+    knobs("ogs.order", 1)
+    knobs("ogs.slab_seg_shift", seg)
+    knobs("ogs.slab_lane", lane)
+    knobs("ogs.slab_defer", 1)
+    ids = O.box_hex_ids(7, 5, 4, 5, 31)
+    h, ref = make(orc, ids)
+    rs, ci = ref["rsT"], ref["ciT"]
+    for dt in (np.float64, np.float32):
+        q = orc.uniform(ids.size, 40).astype(dt)
+        q[::7] = -0.0
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        want = orc.gather_scatter(rs, ci, rs, ci, q)
+        got = host(dq)
+        np.testing.assert_array_equal(got, want)
+        np.testing.assert_array_equal(np.signbit(got), np.signbit(want))
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64, torch.int32, torch.int64])
