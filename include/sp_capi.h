@@ -98,8 +98,9 @@ void        sp_launch_count_reset(void);
  *    at 8 members per lane, else 2) and
  *    "ogs.slab_load" (0..3, default 0: kernel 7's value loads -- 0 plain, 1 L2
  *    only, 2 evict-first, 3 the read-only path for gathers, plain for the in-place
- *    gather+scatter; with the default CTAs), all for the Add op (other ops run the
- *    defaults);
+ *    gather+scatter; with the default CTAs) and "ogs.slab_defer" (1 = kernel 7's
+ *    in-place gather+scatter stores a pass's results after the next pass's loads;
+ *    default 0), all for the Add op (other ops run the defaults);
  *  "ogs.singles" (0..2, default 2; kernel 2 on rows grouped by size: 1 = the
  *    in-place gather+scatter lets the rows of a single member skip the
  *    shared-memory staging and the combine loop -- the lane that gathered such a
