@@ -90,7 +90,11 @@ void        sp_launch_count_reset(void);
  *  "ogs.slabs" (1 = plans created afterwards also hold the slab layouts kernel 7
  *    runs on, about 4 bytes per entry and per row of each walk; default 0: kernel
  *    7 then runs as kernel 2), "ogs.slab_seg_shift" (8..22, default 17: rows are
- *    regrouped by size inside runs of 2^n entries of the walk);
+ *    regrouped by size inside runs of 2^n entries of the walk), "ogs.slab_code_shift"
+ *    (0..12, default 0: with s > 0 a slab whose ids have at most 128 distinct high
+ *    parts id >> s stores them as 16-bit codes (table index << s | low s bits),
+ *    which kernel 7 decodes through the slab's table; s = log2 of the nodes per
+ *    element, e.g. 9 at p = 7, makes a high part an element);
  *  "ogs.slab_lane" (0..16, default 0: members in flight per lane and pass of
  *    kernel 7 -- 0 = 8, and 16 for the gather+scatter of 4-byte values, 1..8 = 8,
  *    9..16 = 16), "ogs.slab_ctas" (0..4, default 0: resident CTAs of 256
@@ -100,7 +104,7 @@ void        sp_launch_count_reset(void);
  *    only, 2 evict-first, 3 the read-only path for gathers, plain for the in-place
  *    gather+scatter; with the default CTAs) and "ogs.slab_defer" (1 = kernel 7's
  *    in-place gather+scatter stores a pass's results after the next pass's loads;
- *    default 0), all for the Add op (other ops run the defaults);
+ *    default 1), all for the Add op (other ops run the defaults);
  *  "ogs.singles" (0..2, default 2; kernel 2 on rows grouped by size: 1 = the
  *    in-place gather+scatter lets the rows of a single member skip the
  *    shared-memory staging and the combine loop -- the lane that gathered such a
@@ -297,6 +301,8 @@ typedef struct {
                          synchronises the device)                                  */
   int32_t NslabsT;    /* lane-row slabs of the main walk (kernel 7; 0: not built)   */
   int32_t NslabsGS;   /* lane-row slabs of the gather+scatter walk (0: none)         */
+  int32_t slabCodeShift;    /* low bits of the slabs' 16-bit member codes (0: none)  */
+  int64_t slabCodedEntries; /* entries of both walks' slabs held as 16-bit codes      */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

@@ -88,11 +88,22 @@ KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift
          "gs_ball_shift": "ogs.gs_ball_shift",
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
          "kernel_scatter": "ogs.kernel.scatter", "scatter_pages": "ogs.scatter_pages",
-         "slabs": "ogs.slabs", "slab_seg_shift": "ogs.slab_seg_shift"}
+         "slabs": "ogs.slabs", "slab_seg_shift": "ogs.slab_seg_shift",
+         "slab_code_shift": "ogs.slab_code_shift"}
 # knobs a table entry may leave out: the library defaults
 PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1, "scatter_pages": 1, "slabs": 0,
-                 "slab_seg_shift": SLAB_SEG_SHIFT}
+                 "slab_seg_shift": SLAB_SEG_SHIFT, "slab_code_shift": 0}
+
+
+def code_shift(p: int) -> int:
+    """Low bits of kernel 7's 16-bit member codes for degree p: enough for the
+    (p+1)^3 nodes of an element, so that a code's high part is an element (at
+    most 12 bits, p <= 15)."""
+    return min(12, max(3, ((p + 1) ** 3 - 1).bit_length()))
 GS_WALK_KERNELS = (1, 2, 3, 5, 7)
+# FP64 times within this fraction of an operation's fastest count as a tie, broken
+# by the FP32 time (the storage form whose kernels differ most)
+FP32_TIE = 0.02
 
 
 def _set(cfg: dict) -> None:
@@ -118,13 +129,16 @@ def _kernels(pc: dict, op: str) -> list[int]:
     return ks
 
 
-def _slabs(choice: dict) -> dict:
-    """A chosen configuration builds the slab layouts only when a kernel 7 uses them."""
+def _slabs(choice: dict, p: int | None = None) -> dict:
+    """A chosen configuration builds the slab layouts only when a kernel 7 uses them
+    (with 16-bit member codes for degree p when p is given)."""
     if 7 in (choice.get("kernel_gather"), choice.get("kernel_gs")):
         choice.update(slabs=1, slab_seg_shift=SLAB_SEG_SHIFT)
+        if p is not None:
+            choice["slab_code_shift"] = code_shift(p)
     else:
-        choice.pop("slabs", None)
-        choice.pop("slab_seg_shift", None)
+        for k in ("slabs", "slab_seg_shift", "slab_code_shift"):
+            choice.pop(k, None)
     return choice
 
 
@@ -134,7 +148,10 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
     operation; the layout with the least BS6 + BS7 + BS8 time wins (the
     gather+scatter may still get a walk of its own afterwards, which is built with
     the chosen layout's row grouping, so its time on the layout counts too).
-    Returns (knobs, BS6 + BS7 ms, BS8 ms)."""
+    Returns (knobs, BS6 + BS7 ms, BS8 ms).  A candidate may carry a ninth field,
+    its time with FP32 values: among the kernels within FP32_TIE of the fastest
+    FP64 time of an operation, the one fastest in FP32 is taken (the FP64 time
+    still decides the layout)."""
     best_key, best, best_main, best_gs_ms = None, None, None, None
     for layout in sorted({t[:4] for t in timings}):
         order, rows, shift, ball = layout
@@ -148,7 +165,11 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
                 t[:4] == layout or t[5] == 0 or
                 (op == "BS7" and t[5] == 5 and t[0] == 0 and t[1] == 0))]
             win = min(cands, key=lambda t: t[7])
-            *_, bnnz, k, _, ms = win
+            near = [t for t in cands if len(t) > 8 and t[8] is not None
+                    and t[7] <= win[7] * (1.0 + FP32_TIE)]
+            if len(near) > 1:
+                win = min(near, key=lambda t: t[8])
+            bnnz, k, ms = win[4], win[5], win[7]
             choice[key] = k
             if op == "BS7" and k == 5:
                 choice["scatter_pages"] = int(win[:4] == layout and order >= 1)
@@ -175,8 +196,10 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
         ids = O.box_hex_ids(E, E, E, p, perm_seed, device="cuda")
     Nt = ids.numel() if isinstance(ids, torch.Tensor) else ids.size
     q = torch.rand(Nt, dtype=torch.float64, device="cuda").to(dtype)
-    timings = []  # (order, rows, page_shift, ball_shift, block_nnz, kernel, op, ms)
-    walk_timings = []  # (gs_order, gs_page_shift, gs_ball_shift, kernel, ms)
+    q32 = q.float() if dtype == torch.float64 else None
+    # (order, rows, page_shift, ball_shift, block_nnz, kernel, op, ms, FP32 ms or None)
+    timings = []
+    walk_timings = []  # (gs_order, gs_page_shift, gs_ball_shift, kernel, ms, FP32 ms or None)
 
     def build():
         h = O.ogs_t()
@@ -184,21 +207,27 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
         return h
 
     try:
-        _set({**PLAN_DEFAULTS, "slabs": 1})
+        _set({**PLAN_DEFAULTS, "slabs": 1, "slab_code_shift": code_shift(p)})
         for pc in plan_configs(p):
             _set(pc)
             h = build()
             gq = torch.zeros(h.Ngather, dtype=dtype, device="cuda")
+            gq32 = torch.zeros(h.Ngather, dtype=torch.float32, device="cuda") if q32 is not None \
+                else None
             ops = {"BS6": lambda: h.Gather(gq, q, 1, O.Add, O.Trans),
                    "BS7": lambda: h.Scatter(q, gq, 1, O.NoTrans),
                    "BS8": lambda: h.GatherScatter(q, 1, O.Add, O.Sym)}
+            ops32 = {"BS6": lambda: h.Gather(gq32, q32, 1, O.Add, O.Trans),
+                     "BS8": lambda: h.GatherScatter(q32, 1, O.Add, O.Sym)}
             for op, key in OPS:
                 for k in _kernels(pc, op):
                     _set({key: k, "scatter_pages": 1})
+                    ms32 = _time(ops32[op], reps, stream) if q32 is not None and op in ops32 \
+                        else None
                     timings.append((pc["order"], pc["rows"], pc["page_shift"], pc["ball_shift"],
-                                    pc["block_nnz"], k, op, _time(ops[op], reps, stream)))
+                                    pc["block_nnz"], k, op, _time(ops[op], reps, stream), ms32))
             h.Free()
-            del gq
+            del gq, gq32
         # the main walk serves the gathers and scatters; the gather+scatter may get
         # a walk of its own below, so it decides the main walk only on a tie
         best, main_ms, best_gs_ms = choose(timings)
@@ -210,26 +239,39 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                 h = build()
                 for k in GS_WALK_KERNELS:
                     _set({"kernel_gs": k})
+                    ms32 = _time(lambda: h.GatherScatter(q32, 1, O.Add, O.Sym), reps, stream) \
+                        if q32 is not None else None
                     walk_timings.append((w["gs_order"], w["gs_page_shift"], w["gs_ball_shift"], k,
                                          _time(lambda: h.GatherScatter(q, 1, O.Add, O.Sym), reps,
-                                               stream)))
+                                               stream), ms32))
                 h.Free()
         best["gs_order"] = -1
         if walk_timings:
-            go, gp, gb, k, ms = min(walk_timings, key=lambda t: t[4])
-            if ms < best_gs_ms:
+            # the chosen layout's own gather+scatter against the walks, with the same
+            # FP32 tie-break as choose()
+            own = next((t for t in timings if t[:4] == (best["order"], best["rows"],
+                                                       best["page_shift"], best["ball_shift"])
+                        and t[6] == "BS8" and t[5] == best["kernel_gs"]), None)
+            cands = [(t[4], t[5], t[:4]) for t in walk_timings]
+            cands.append((best_gs_ms, own[8] if own is not None and len(own) > 8 else None, None))
+            win = min(cands, key=lambda c: c[0])
+            near = [c for c in cands if c[1] is not None and c[0] <= win[0] * (1.0 + FP32_TIE)]
+            if len(near) > 1:
+                win = min(near, key=lambda c: c[1])
+            if win[2] is not None:
+                go, gp, gb, k = win[2]
                 best.update(gs_order=go, gs_page_shift=gp, gs_ball_shift=gb, kernel_gs=k)
-                best_total += ms - best_gs_ms
-        _slabs(best)
+                best_total += win[0] - best_gs_ms
+        _slabs(best, p)
     finally:
         _set(saved)
     return {"p": p, "E": E, "perm": bool(perm_seed), "local_nodes": int(Nt), "best": best,
             "best_total_ms": best_total,
             "candidates": [{"order": o, "rows": r, "page_shift": ps, "ball_shift": bs,
-                            "block_nnz": b, "kernel": k, "op": op, "ms": ms}
-                           for o, r, ps, bs, b, k, op, ms in timings],
+                            "block_nnz": b, "kernel": k, "op": op, "ms": ms, "ms_fp32": ms32}
+                           for o, r, ps, bs, b, k, op, ms, ms32 in timings],
             "gs_walks": [{"gs_order": o, "gs_page_shift": ps, "gs_ball_shift": bs, "kernel": k,
-                          "ms": ms} for o, ps, bs, k, ms in walk_timings]}
+                          "ms": ms, "ms_fp32": ms32} for o, ps, bs, k, ms, ms32 in walk_timings]}
 
 
 def load_table(path: Path = TABLE) -> dict:

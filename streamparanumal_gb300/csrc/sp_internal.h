@@ -65,6 +65,7 @@ enum TuneKey : int {
   kTuneOgsSlabCtas,         // kernel 7: resident CTAs per SM (0 = 2, 1..4)
   kTuneOgsSlabLoad,         // kernel 7: value loads 0 plain, 1 L2 only, 2 evict-first, 3 read-only path
   kTuneOgsSlabDefer,        // kernel 7 gather+scatter: 1 = a pass's stores after the next pass's loads
+  kTuneOgsSlabCodeShift,    // ogs plan: 0 = 32-bit slab ids, 6..12 = 16-bit codes with that many low bits
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -937,10 +937,7 @@ struct ChunkArgs {
   const int32_t* perm;  // walk row -> row of the operator (renumbered walk only)
   int32_t* waitErr;      // the plan's count of bounded waits that gave up
   const int2* sing;      // per chunk (multi-member rows, their entries), grouped rows only
-  const int4* slabs;     // lane-row slabs of the same walk (kernel 7), else null
-  int32_t nslabs;
-  const int32_t* slabIds;
-  const int32_t* slabRows;
+  SlabArgs slab;          // lane-row slabs of the same walk (kernel 7); slabs null if none
 };
 static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
   const bool g = p->row_order == 1;
@@ -950,8 +947,9 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
                    g ? p->d_rowsGT : rs, g ? p->d_colIdsGT : ci, g ? 1 : 0,
                    p->d_colIdsST, p->d_e2sT, p->d_permT, p->d_waitErr,
                    g ? reinterpret_cast<const int2*>(p->d_singT) : nullptr,
-                   reinterpret_cast<const int4*>(p->d_slabsT), p->nslabsT, p->d_slabIdsT,
-                   p->d_slabRowsT};
+                   SlabArgs{reinterpret_cast<const int4*>(p->d_slabsT), p->nslabsT, p->d_slabIdsT,
+                            p->d_slabRowsT, p->d_slabCodesT, p->d_slabTabsT,
+                            reinterpret_cast<const int2*>(p->d_slabTdT), p->slab_code_shift}};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -961,13 +959,14 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksGS), p->nchunksGS, rs, ci,
                    p->gs_grouped, nullptr, nullptr, nullptr, p->d_waitErr,
                    p->gs_grouped ? reinterpret_cast<const int2*>(p->d_singGS) : nullptr,
-                   reinterpret_cast<const int4*>(p->d_slabsGS), p->nslabsGS, p->d_slabIdsGS,
-                   nullptr};
+                   SlabArgs{reinterpret_cast<const int4*>(p->d_slabsGS), p->nslabsGS,
+                            p->d_slabIdsGS, nullptr, p->d_slabCodesGS, p->d_slabTabsGS,
+                            reinterpret_cast<const int2*>(p->d_slabTdGS), p->slab_code_shift}};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
                    p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr, nullptr,
-                   nullptr, 0, nullptr, nullptr};
+                   SlabArgs{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0}};
 }
 
 // Kernel 6: the pipelined persistent gathers of kernel 2 with the chunks' column ids
@@ -1090,10 +1089,10 @@ static void launch_chunked_gather(int kv, const ChunkArgs& a, T* v, T* gv, cudaS
   const bool perm = MODE == 1 && a.perm;
   if (perm && (kv == 3 || kv == 4)) kv = 2;
   if (kv == 6 && !a.waitErr) kv = 2;  // a plan without chunks has no wait-error word
-  if (kv == 7 && !a.slabs) kv = 2;     // a plan built without slabs (ogs.slabs = 0)
+  if (kv == 7 && !a.slab.slabs) kv = 2;  // a plan built without slabs (ogs.slabs = 0)
   const unsigned pg = persistent_grid(a.nchunks, kOgsPersistentCtas);
   if (kv == 7) {
-    launch_slabs<T, OP, MODE>(a.slabs, a.nslabs, a.slabIds, a.slabRows, v, gv, s);
+    launch_slabs<T, OP, MODE>(a.slab, v, gv, s);
   } else if (kv == 6) {
     launch_bulk_gather<T, OP, MODE>(a, v, gv, perm, s);
   } else if (kv == 5) {
@@ -1372,10 +1371,17 @@ static void free_plan_device(sp_ogs_plan* p) {
   p->nchunksGS = p->gs_grouped = 0;
   if (p->d_waitErr) cudaFree(p->d_waitErr);
   p->d_waitErr = nullptr;
-  for (int32_t* q : {p->d_slabsT, p->d_slabIdsT, p->d_slabRowsT, p->d_slabsGS, p->d_slabIdsGS})
+  for (int32_t* q : {p->d_slabsT, p->d_slabIdsT, p->d_slabRowsT, p->d_slabsGS, p->d_slabIdsGS,
+                     p->d_slabTabsT, p->d_slabTdT, p->d_slabTabsGS, p->d_slabTdGS})
+    if (q) cudaFree(q);
+  for (uint16_t* q : {p->d_slabCodesT, p->d_slabCodesGS})
     if (q) cudaFree(q);
   p->d_slabsT = p->d_slabIdsT = p->d_slabRowsT = p->d_slabsGS = p->d_slabIdsGS = nullptr;
+  p->d_slabTabsT = p->d_slabTdT = p->d_slabTabsGS = p->d_slabTdGS = nullptr;
+  p->d_slabCodesT = p->d_slabCodesGS = nullptr;
   p->nslabsT = p->nslabsGS = 0;
+  p->slab_code_shift = 0;
+  p->slab_coded_entries = 0;
   if (p->d_singT) cudaFree(p->d_singT);
   if (p->d_singGS) cudaFree(p->d_singGS);
   p->d_singT = p->d_singGS = nullptr;
@@ -1435,11 +1441,13 @@ static std::vector<int32_t> singleton_split(const std::vector<int32_t>& quads,
 }
 
 // Slab layout of one walk (build_slabs), uploaded; `rows_out` null for a walk that
-// only serves the in-place gather+scatter.
-static sp_status build_slab_layout(const std::vector<int32_t>& quads, const int32_t* wrs,
-                                   const int32_t* wci, const int32_t* perm, bool with_rows,
-                                   int32_t** desc_out, int32_t** ids_out, int32_t** rows_out,
-                                   int32_t* nslabs, cudaStream_t s) {
+// only serves the in-place gather+scatter.  With ogs.slab_code_shift > 0 also the
+// 16-bit codes of the slabs that compress (compress_slabs).
+static sp_status build_slab_layout(sp_ogs_plan* p, const std::vector<int32_t>& quads,
+                                   const int32_t* wrs, const int32_t* wci, const int32_t* perm,
+                                   bool with_rows, int32_t** desc_out, int32_t** ids_out,
+                                   int32_t** rows_out, int32_t* nslabs, uint16_t** codes_out,
+                                   int32_t** tabs_out, int32_t** td_out, cudaStream_t s) {
   std::vector<int32_t> desc, ids, rows;
   build_slabs(quads, wrs, wci, perm, (int)tune(kTuneOgsSlabSegShift), with_rows, desc, ids,
               rows);
@@ -1448,6 +1456,23 @@ static sp_status build_slab_layout(const std::vector<int32_t>& quads, const int3
   if ((st = upload(ids, ids_out, s))) return st;
   if (rows_out && (st = upload(rows, rows_out, s))) return st;
   *nslabs = (int32_t)(desc.size() / 4);
+  const int shift = (int)tune(kTuneOgsSlabCodeShift);
+  if (shift > 0 && *nslabs > 0) {
+    std::vector<uint16_t> codes;
+    std::vector<int32_t> tabs, td;
+    compress_slabs(desc, ids, shift, codes, tabs, td);
+    if ((st = upload(codes, codes_out, s))) return st;
+    if ((st = upload(tabs, tabs_out, s))) return st;
+    if ((st = upload(td, td_out, s))) return st;
+    p->slab_code_shift = shift;
+    for (int32_t g = 0; g < *nslabs; ++g)
+      if (td[2 * g + 1] > 0) {
+        const int32_t w = desc[4 * g + 3];
+        p->slab_coded_entries +=
+            (int64_t)(((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255)) * desc[4 * g + 2];
+      }
+    SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+  }
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
 }
@@ -1496,8 +1521,9 @@ static sp_status build_gs_walk(sp_ogs_plan* p, cudaStream_t s) {
   }
   p->nchunksGS = (int32_t)(quads.size() / 4);
   if (tune(kTuneOgsSlabs) == 1 &&
-      (st = build_slab_layout(quads, wrs, wci, nullptr, false, &p->d_slabsGS, &p->d_slabIdsGS,
-                              nullptr, &p->nslabsGS, s)))
+      (st = build_slab_layout(p, quads, wrs, wci, nullptr, false, &p->d_slabsGS,
+                              &p->d_slabIdsGS, nullptr, &p->nslabsGS, &p->d_slabCodesGS,
+                              &p->d_slabTabsGS, &p->d_slabTdGS, s)))
     return st;
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
@@ -1676,8 +1702,9 @@ sp_status finalize_plan(sp_ogs_plan* p, cudaStream_t s) {
     }
     // lane-row slabs of the main walk (kernel 7)
     if (tune(kTuneOgsSlabs) == 1 && p->nchunksT > 0 &&
-        (st = build_slab_layout(chunksT, wrs, wci, renumber ? perm.data() : nullptr, true,
-                                &p->d_slabsT, &p->d_slabIdsT, &p->d_slabRowsT, &p->nslabsT, s)))
+        (st = build_slab_layout(p, chunksT, wrs, wci, renumber ? perm.data() : nullptr, true,
+                                &p->d_slabsT, &p->d_slabIdsT, &p->d_slabRowsT, &p->nslabsT,
+                                &p->d_slabCodesT, &p->d_slabTabsT, &p->d_slabTdT, s)))
       return st;
     // T chunk entries in column order: the column-order scatter and gathers
     std::vector<int32_t> colS;
@@ -1796,6 +1823,8 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->pageShift = p->pages_shift;
   info->NslabsT = p->nslabsT;
   info->NslabsGS = p->nslabsGS;
+  info->slabCodeShift = p->slab_code_shift;
+  info->slabCodedEntries = p->slab_coded_entries;
   info->waitErrors = 0;
   if (p->d_waitErr) {
     int32_t* dev = p->d_waitErr;

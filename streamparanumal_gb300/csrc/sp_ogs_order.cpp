@@ -512,4 +512,61 @@ void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int
   }
 }
 
+void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>& ids, int shift,
+                    std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
+                    std::vector<int32_t>& tdesc) {
+  const int64_t nslabs = (int64_t)desc.size() / 4;
+  const int32_t maxTab = std::min<int32_t>(kSlabCodeTable, 1 << (16 - shift));
+  const int32_t mask = (1 << shift) - 1;
+  codes.assign(ids.size(), 0);
+  tdesc.assign(2 * std::max<int64_t>(nslabs, 1), -1);
+  std::vector<int32_t> ntab(nslabs + 1, 0);
+  // pass 1: the distinct high parts of each slab (first-appearance order), codes
+#pragma omp parallel
+  {
+    std::vector<int32_t> tab;
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t g = 0; g < nslabs; ++g) {
+      const int32_t E = desc[4 * g], m = desc[4 * g + 2], w = desc[4 * g + 3];
+      const int32_t nl = w & 255, rem = (w >> 8) & 255, Re = w >> 16;
+      const int64_t n = (int64_t)((Re - 1) * nl + rem) * m;
+      tab.clear();
+      bool ok = m > 0;
+      for (int64_t k = 0; k < n && ok; ++k) {
+        const int32_t hi = ids[E + k] >> shift;
+        int32_t t = 0;
+        while (t < (int32_t)tab.size() && tab[t] != hi) ++t;
+        if (t == (int32_t)tab.size()) {
+          if ((int32_t)tab.size() == maxTab) ok = false;
+          else tab.push_back(hi);
+        }
+        if (ok) codes[E + k] = (uint16_t)((t << shift) | (ids[E + k] & mask));
+      }
+      ntab[g + 1] = ok ? (int32_t)tab.size() : 0;
+      tdesc[2 * g + 1] = ok ? (int32_t)tab.size() : 0;
+    }
+  }
+  for (int64_t g = 0; g < nslabs; ++g) ntab[g + 1] += ntab[g];
+  tables.assign(std::max<int32_t>(ntab[nslabs], 1), 0);
+  // pass 2: the tables (high part << shift), and each compressed slab's offset
+#pragma omp parallel
+  {
+    std::vector<int32_t> tab;
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t g = 0; g < nslabs; ++g) {
+      if (tdesc[2 * g + 1] == 0) continue;
+      const int32_t E = desc[4 * g], m = desc[4 * g + 2], w = desc[4 * g + 3];
+      const int32_t nl = w & 255, rem = (w >> 8) & 255, Re = w >> 16;
+      const int64_t n = (int64_t)((Re - 1) * nl + rem) * m;
+      tab.clear();
+      for (int64_t k = 0; k < n; ++k) {
+        const int32_t hi = ids[E + k] >> shift;
+        if (std::find(tab.begin(), tab.end(), hi) == tab.end()) tab.push_back(hi);
+      }
+      for (size_t t = 0; t < tab.size(); ++t) tables[ntab[g] + t] = tab[t] << shift;
+      tdesc[2 * g] = ntab[g];
+    }
+  }
+}
+
 }  // namespace sp

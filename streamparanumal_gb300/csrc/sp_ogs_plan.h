@@ -102,6 +102,18 @@ void build_sorted(const std::vector<int32_t>& quads, int32_t nrows, const int32_
 // without members, as slabs of m = 0).  Each row keeps its members in CSR order.
 constexpr int32_t kSlabLaneEntries = 16;
 int32_t slab_rows_per_lane(int32_t m);
+
+// 16-bit member ids for slabs (ogs.slab_code_shift = s): a slab whose ids have at
+// most kSlabCodeTable distinct high parts (id >> s; and at most 2^(16-s)) stores
+// each id as code = (index of its high part in the slab's table) << s | (id's low s
+// bits), at the id's own position in `codes`; tables[tdesc[2g] + t] = high part t
+// << s.  tdesc[2g + 1] = the table's length, 0 for a slab left uncompressed
+// (tdesc[2g] = -1; it keeps its 32-bit ids).  On a box mesh of (p+1)^3 = 2^s local
+// nodes per element a high part is an element, and a slab touches a few of them.
+constexpr int32_t kSlabCodeTable = 128;
+void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>& ids, int shift,
+                    std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
+                    std::vector<int32_t>& tdesc);
 void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
                  const int32_t* perm, int seg_shift, bool with_rows, std::vector<int32_t>& desc,
                  std::vector<int32_t>& ids, std::vector<int32_t>& rows);
@@ -194,6 +206,15 @@ struct sp_ogs_plan {
   int32_t* d_slabsGS = nullptr;
   int32_t* d_slabIdsGS = nullptr;
   int32_t nslabsGS = 0;
+  // their 16-bit member codes (compress_slabs; null unless ogs.slab_code_shift > 0)
+  uint16_t* d_slabCodesT = nullptr;
+  int32_t* d_slabTabsT = nullptr;
+  int32_t* d_slabTdT = nullptr;
+  uint16_t* d_slabCodesGS = nullptr;
+  int32_t* d_slabTabsGS = nullptr;
+  int32_t* d_slabTdGS = nullptr;
+  int32_t slab_code_shift = 0;
+  int64_t slab_coded_entries = 0;   // entries in compressed slabs, both walks
   // count of bounded device waits that gave up (the bulk-staged gathers' waits)
   int32_t* d_waitErr = nullptr;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations

@@ -238,29 +238,60 @@ __device__ __forceinline__ T load_val(const T* p) {
   else return *p;
 }
 
+// The member ids of a lane's full pass starting at step j of slab e: 32-bit ids, or
+// the 16-bit codes of a compressed slab (decoded against its table later).
+template <int KB>
+__device__ __forceinline__ void load_raw(const int32_t* __restrict__ ids,
+                                         const uint16_t* __restrict__ codes, int4 e, int j,
+                                         bool coded, int lane, int32_t (&raw)[KB]) {
+  const int32_t off = e.x + j * e.z * 32 + lane;
+  if (coded) {
+#pragma unroll
+    for (int u = 0; u < KB; ++u) raw[u] = (int32_t)__ldg(codes + off + 32 * u);
+  } else {
+#pragma unroll
+    for (int u = 0; u < KB; ++u) raw[u] = __ldg(ids + off + 32 * u);
+  }
+}
+
 // DF = 1 (gather+scatter only): a full pass's stores are issued after the next
-// pass's value loads.
+// pass's value loads.  With `codes` (ogs.slab_code_shift > 0) the slabs that
+// compressed read 16-bit member codes, decoded through their table of high parts,
+// which the warp keeps in shared memory (loaded one slab ahead into registers,
+// stored when the slab begins); the other slabs read their 32-bit ids.
 template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
 __global__ void __launch_bounds__(kOgsThreads, CTAS)
 k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __restrict__ ids,
-              const int32_t* __restrict__ rows, T* v, T* gv) {
+              const int32_t* __restrict__ rows, T* v, T* gv, const uint16_t* __restrict__ codes,
+              const int32_t* __restrict__ tabs, const int2* __restrict__ td, int sh) {
+  __shared__ int32_t stab[kWarpsPerCta][kSlabCodeTable];
   constexpr bool defer = DF != 0 && MODE == 0;
+  constexpr int TPL = kSlabCodeTable / 32;  // table words per lane
   T pval[KB];
   int32_t pcid[KB];
   uint32_t pm = 0u;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t W = gridDim.x * kWarpsPerCta;
-  int32_t s = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  int32_t s = blockIdx.x * kWarpsPerCta + w;
   if (s >= nslabs) return;
   const int4 zero = make_int4(0, 0, 0, 0);
+  const int2 plain = make_int2(-1, 0);
+  const int32_t mask = (1 << sh) - 1;
   int4 d = __ldg(slabs + s);
   int4 dn = (s + W < nslabs) ? __ldg(slabs + s + W) : zero;
+  int2 t = codes ? __ldg(td + s) : plain;
+  int2 tn = (codes && s + W < nslabs) ? __ldg(td + s + W) : plain;
   int j0 = 0;
   bool full = pass_full<KB>(d, 0);
-  int32_t cid[KB];
+  int32_t raw[KB];
   if (full) {
+    load_raw<KB>(ids, codes, d, 0, t.y > 0, lane, raw);
+    if (t.y > 0) {
 #pragma unroll
-    for (int u = 0; u < KB; ++u) cid[u] = __ldg(ids + d.x + lane + 32 * u);
+      for (int i = 0; i < TPL; ++i)
+        if (lane + 32 * i < t.y) stab[w][lane + 32 * i] = __ldg(tabs + t.x + lane + 32 * i);
+      __syncwarp();
+    }
   }
   while (true) {
     const int m = d.z, Re = d.w >> 16;
@@ -268,11 +299,21 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
     // the pass after this one: the next steps of this slab, or the next slab
     const bool next_slab = !full || j0 + P >= Re;
     const int4 dx = next_slab ? dn : d;
+    const int2 tx = next_slab ? tn : t;
     const int jx = next_slab ? 0 : j0 + P;
     const bool has_next = !next_slab || s + W < nslabs;
     const bool fullx = has_next && pass_full<KB>(dx, jx);
-    int32_t nid[KB];
+    int32_t nraw[KB];
+    int32_t ntab[TPL];
     if (full) {
+      int32_t cid[KB];
+      if (t.y > 0) {
+#pragma unroll
+        for (int u = 0; u < KB; ++u) cid[u] = stab[w][raw[u] >> sh] | (raw[u] & mask);
+      } else {
+#pragma unroll
+        for (int u = 0; u < KB; ++u) cid[u] = raw[u];
+      }
       T val[KB];
       int32_t rw[KB];
 #pragma unroll
@@ -284,9 +325,12 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
           if (jj < P) rw[jj] = __ldg(rsrc + 32 * jj);
       }
       if (fullx) {
-        const int32_t* src = ids + dx.x + jx * dx.z * 32 + lane;
+        load_raw<KB>(ids, codes, dx, jx, tx.y > 0, lane, nraw);
+        if (next_slab && tx.y > 0) {
 #pragma unroll
-        for (int u = 0; u < KB; ++u) nid[u] = __ldg(src + 32 * u);
+          for (int i = 0; i < TPL; ++i)
+            if (lane + 32 * i < tx.y) ntab[i] = __ldg(tabs + tx.x + lane + 32 * i);
+        }
       }
       if constexpr (defer) {
         flush_deferred<T, KB>(v, pval, pcid, pm);
@@ -308,62 +352,76 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
       if constexpr (defer) flush_deferred<T, KB>(v, pval, pcid, pm);
       slab_rest<T, OP, MODE, KB>(ids, rows, v, gv, d, j0, lane);
       if (fullx) {
-        const int32_t* src = ids + dx.x + jx * dx.z * 32 + lane;
+        load_raw<KB>(ids, codes, dx, jx, tx.y > 0, lane, nraw);
+        if (next_slab && tx.y > 0) {
 #pragma unroll
-        for (int u = 0; u < KB; ++u) nid[u] = __ldg(src + 32 * u);
+          for (int i = 0; i < TPL; ++i)
+            if (lane + 32 * i < tx.y) ntab[i] = __ldg(tabs + tx.x + lane + 32 * i);
+        }
       }
     }
     if (!has_next) break;
     if (next_slab) {
       s += W;
       d = dn;
+      t = tn;
       dn = (s + W < nslabs) ? __ldg(slabs + s + W) : zero;
+      tn = (codes && s + W < nslabs) ? __ldg(td + s + W) : plain;
     }
     j0 = jx;
     full = fullx;
     if (full) {
 #pragma unroll
-      for (int u = 0; u < KB; ++u) cid[u] = nid[u];
+      for (int u = 0; u < KB; ++u) raw[u] = nraw[u];
+      if (next_slab && t.y > 0) {
+        __syncwarp();  // every lane has decoded its last pass against the old table
+#pragma unroll
+        for (int i = 0; i < TPL; ++i)
+          if (lane + 32 * i < t.y) stab[w][lane + 32 * i] = ntab[i];
+        __syncwarp();
+      }
     }
   }
   if constexpr (defer) flush_deferred<T, KB>(v, pval, pcid, pm);
 }
 
 template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
-static void launch_shape(const int4* slabs, int32_t nslabs, const int32_t* ids,
-                         const int32_t* rows, T* v, T* gv, cudaStream_t s) {
+static void launch_shape(const SlabArgs& a, T* v, T* gv, cudaStream_t s) {
+  const int4* slabs = a.slabs;
+  const int32_t nslabs = a.nslabs;
   const int64_t want = ((int64_t)nslabs + kWarpsPerCta - 1) / kWarpsPerCta;
   const int64_t cap = (int64_t)sm_count() * CTAS;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min(want, cap));
-  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD, DF><<<g, kOgsThreads, 0, s>>>(slabs, nslabs, ids, rows,
-                                                                     v, gv);
+  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD, DF><<<g, kOgsThreads, 0, s>>>(
+      slabs, nslabs, a.ids, a.rows, v, gv, a.codes, a.tabs, a.td, a.shift);
 }
 
 // One pass size with the resident CTAs the knob ogs.slab_ctas asks for (Add only;
 // 0 = the shape's default).
 template <typename T, int OP, int MODE, int KB>
-static void launch_ctas(const int4* slabs, int32_t nslabs, const int32_t* ids,
-                        const int32_t* rows, T* v, T* gv, cudaStream_t s) {
+static void launch_ctas(const SlabArgs& a, T* v, T* gv, cudaStream_t s) {
   constexpr int dflt = SlabCtas<(int)sizeof(T), KB>::value;
+  // deferred stores (default on): with the 16-bit codes they took the FP64 in-place
+  // gather+scatter +5 % and FP32 +14 % on 64^3 p = 7 boxes, p = 15 within +-2 %
   if constexpr (OP == SP_OP_ADD && MODE == 0) {
     if (tune(kTuneOgsSlabDefer) == 1)
-      return launch_shape<T, OP, MODE, KB, dflt, 0, 1>(slabs, nslabs, ids, rows, v, gv, s);
+      return launch_shape<T, OP, MODE, KB, dflt, 0, 1>(a, v, gv, s);
   }
   if constexpr (OP == SP_OP_ADD) {
     switch (tune(kTuneOgsSlabLoad)) {
-      case 1: return launch_shape<T, OP, MODE, KB, dflt, 1>(slabs, nslabs, ids, rows, v, gv, s);
-      case 2: return launch_shape<T, OP, MODE, KB, dflt, 2>(slabs, nslabs, ids, rows, v, gv, s);
-      case 3: return launch_shape<T, OP, MODE, KB, dflt, 3>(slabs, nslabs, ids, rows, v, gv, s);
+      case 1: return launch_shape<T, OP, MODE, KB, dflt, 1>(a, v, gv, s);
+      case 2: return launch_shape<T, OP, MODE, KB, dflt, 2>(a, v, gv, s);
+      case 3: return launch_shape<T, OP, MODE, KB, dflt, 3>(a, v, gv, s);
       default: break;
     }
     switch (tune(kTuneOgsSlabCtas)) {
-      case 1: return launch_shape<T, OP, MODE, KB, 1>(slabs, nslabs, ids, rows, v, gv, s);
-      case 3: return launch_shape<T, OP, MODE, KB, 3>(slabs, nslabs, ids, rows, v, gv, s);
-      case 4: return launch_shape<T, OP, MODE, KB, 4>(slabs, nslabs, ids, rows, v, gv, s);
+      case 1: return launch_shape<T, OP, MODE, KB, 1>(a, v, gv, s);
+      case 3: return launch_shape<T, OP, MODE, KB, 3>(a, v, gv, s);
+      case 4: return launch_shape<T, OP, MODE, KB, 4>(a, v, gv, s);
       default: break;
     }
   }
-  launch_shape<T, OP, MODE, KB, dflt>(slabs, nslabs, ids, rows, v, gv, s);
+  launch_shape<T, OP, MODE, KB, dflt>(a, v, gv, s);
 }
 
 // Members in flight per lane and pass: 8, except 16 for the in-place
@@ -372,24 +430,21 @@ static void launch_ctas(const int4* slabs, int32_t nslabs, const int32_t* ids,
 // 16 at 2 +3 % over 8 at 3); 8 or 16 when the knob says so.  The other shape is
 // compiled for Add, the op the benchmarks time; the other ops run the default.
 template <typename T, int OP, int MODE>
-void launch_slabs(const int4* slabs, int32_t nslabs, const int32_t* ids, const int32_t* rows,
-                  T* v, T* gv, cudaStream_t s) {
-  if (nslabs <= 0) return;
+void launch_slabs(const SlabArgs& a, T* v, T* gv, cudaStream_t s) {
+  if (a.nslabs <= 0) return;
   constexpr int KB = (sizeof(T) == 4 && MODE == 0) ? 16 : 8;
   constexpr int KO = KB == 16 ? 8 : 16;
   if constexpr (OP == SP_OP_ADD) {
     const int64_t lane = tune(kTuneOgsSlabLane);
     if (lane > 0 && (lane <= 8 ? 8 : 16) == KO)
-      return launch_ctas<T, OP, MODE, KO>(slabs, nslabs, ids, rows, v, gv, s);
+      return launch_ctas<T, OP, MODE, KO>(a, v, gv, s);
   }
-  launch_ctas<T, OP, MODE, KB>(slabs, nslabs, ids, rows, v, gv, s);
+  launch_ctas<T, OP, MODE, KB>(a, v, gv, s);
 }
 
-#define SP_SLAB_INST(T, OP)                                                                    \
-  template void launch_slabs<T, OP, 0>(const int4*, int32_t, const int32_t*, const int32_t*, T*, \
-                                       T*, cudaStream_t);                                      \
-  template void launch_slabs<T, OP, 1>(const int4*, int32_t, const int32_t*, const int32_t*, T*, \
-                                       T*, cudaStream_t);
+#define SP_SLAB_INST(T, OP)                                                   \
+  template void launch_slabs<T, OP, 0>(const SlabArgs&, T*, T*, cudaStream_t); \
+  template void launch_slabs<T, OP, 1>(const SlabArgs&, T*, T*, cudaStream_t);
 #define SP_SLAB_INST_OPS(T) \
   SP_SLAB_INST(T, SP_OP_ADD) SP_SLAB_INST(T, SP_OP_MUL) SP_SLAB_INST(T, SP_OP_MAX) \
   SP_SLAB_INST(T, SP_OP_MIN)

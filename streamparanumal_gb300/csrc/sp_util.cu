@@ -56,7 +56,8 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.slab_lane", 0, 16, {0}},
     {"ogs.slab_ctas", 0, 4, {0}},
     {"ogs.slab_load", 0, 3, {0}},
-    {"ogs.slab_defer", 0, 1, {0}},
+    {"ogs.slab_defer", 0, 1, {1}},
+    {"ogs.slab_code_shift", 0, 12, {0}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

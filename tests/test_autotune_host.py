@@ -65,6 +65,8 @@ def test_committed_table_is_well_formed():
         # the slab layouts are built exactly where a kernel 7 runs on them
         uses = 7 in (cfg["kernel_gather"], cfg["kernel_gs"])
         assert cfg.get("slabs", 0) == int(uses)
+        p = int(key[1:].split("_")[0])
+        assert cfg.get("slab_code_shift", 0) == (autotune.code_shift(p) if uses else 0)
 
 
 def test_text_form_matches_the_table():
@@ -141,3 +143,22 @@ def test_choose_counts_the_gather_scatter_time_of_each_layout():
     # (BS7 takes the memory-order column-major scatter of the plain plan, which
     # competes under every layout)
     assert best["kernel_gs"] == 2 and abs(main - 0.85) < 1e-12 and gs == 0.5
+
+
+def test_code_shift_covers_an_element():
+    assert [autotune.code_shift(p) for p in (1, 2, 3, 5, 7, 9, 15)] == [3, 5, 6, 8, 9, 10, 12]
+    for p in range(1, 16):
+        assert (p + 1) ** 3 <= 1 << autotune.code_shift(p)
+
+
+def test_choose_breaks_near_ties_by_the_fp32_time():
+    walk = (1, 1, 9, 19, 2048)
+    t = [x + (None,) for x in _timings({walk + (2, "BS6"): 0.500, walk + (7, "BS6"): 0.505})]
+    t = [x[:8] + ((0.30 if x[5] == 7 else 0.40),) if x[:7] in (walk + (2, "BS6"), walk + (7, "BS6"))
+         else x for x in t]
+    best, _, _ = autotune.choose(t)
+    assert best["kernel_gather"] == 7 and best["slabs"] == 1
+    # outside the tie band the FP64 time decides
+    t = [x[:7] + (0.52 if x[:7] == walk + (7, "BS6") else x[7], x[8]) for x in t]
+    best, _, _ = autotune.choose(t)
+    assert best["kernel_gather"] == 2 and "slabs" not in best

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
          "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.slabs", "ogs.slab_seg_shift",
          "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.slab_defer",
-         "ogs.page_shift", "ogs.ball_shift")
+         "ogs.slab_code_shift", "ogs.page_shift", "ogs.ball_shift")
 
 
 @pytest.fixture
@@ -148,12 +148,43 @@ def test_slab_deferred_stores(cuda, orc, knobs, seg, lane):
         np.testing.assert_array_equal(np.signbit(got), np.signbit(want))
 
 
+@pytest.mark.parametrize("box,shift", [((5, 4, 3, 7, 2024), 9), ((6, 6, 6, 2, 5), 5),
+                                       ((9, 8, 7, 5, 3), 8), ((7, 3, 2, 1, 0), 3),
+                                       ((4, 3, 5, 3, 77), 12), ((16, 16, 16, 7, 0), 6)])
+@pytest.mark.parametrize("order,gs_order", [(1, -1), (2, 2)])
+def test_slabs_with_16bit_codes(cuda, orc, knobs, box, shift, order, gs_order):
+    """Slabs whose ids fit 16-bit codes (ogs.slab_code_shift) decode them through the
+    slab's table in shared memory; the others keep 32-bit ids: the same bits for
+    the gather and the gather+scatter, FP64 and FP32, with the deferred stores too."""
+    nx, ny, nz, p, seed = box
+    knobs("ogs.order", order)
+    knobs("ogs.gs_order", gs_order)
+    knobs("ogs.gs_page_shift", 6)
+    knobs("ogs.gs_ball_shift", 0)
+    knobs("ogs.slab_code_shift", shift)
+    ids = O.box_hex_ids(nx, ny, nz, p, seed)
+    h, ref = make(orc, ids)
+    assert h.info.slabCodeShift == shift and h.info.slabCodedEntries > 0
+    check_fp64(orc, h, ref, ids.size, 11 + p)
+    rs, ci = ref["rsT"], ref["ciT"]
+    q = orc.uniform(ids.size, 12).astype(np.float32)
+    gq = torch.zeros(rs.size - 1, dtype=torch.float32, device="cuda")
+    h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+    np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
+    for defer in (0, 1):
+        knobs("ogs.slab_defer", defer)
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+
+
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64, torch.int32, torch.int64])
 @pytest.mark.parametrize("op", [O.Add, O.Mul, O.Max, O.Min])
 @pytest.mark.parametrize("lane", [0, 16])
 def test_slabs_types_ops(cuda, orc, knobs, dtype, op, lane):
     knobs("ogs.order", 1)
     knobs("ogs.slab_lane", lane)
+    knobs("ogs.slab_code_shift", 6 if lane else 0)
     ids = O.box_hex_ids(4, 3, 5, 3, 77)
     h, ref = make(orc, ids)
     rs, ci = ref["rsT"], ref["ciT"]
