@@ -19,7 +19,11 @@
 // Persistent warps take slabs s, s + W, s + 2W, ... (W warps in the grid), so the
 // slabs in flight at any moment are a window of the walk, as for the chunk
 // kernels.  A slab is worked in passes of KB members per lane; the ids of the next
-// pass load while the current pass's values are in flight.
+// pass load while the current pass's values are in flight.  Slabs may carry their
+// ids as 16-bit element-relative codes (compress_slabs), decoded through a table
+// the warp keeps in shared memory, and the in-place gather+scatter may defer a
+// pass's stores until the next pass's loads are issued.  Every choice computes the
+// same bits.
 #include <algorithm>
 
 #include "sp_internal.h"
