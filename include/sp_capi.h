@@ -86,7 +86,9 @@ void        sp_launch_count_reset(void);
  *    pipelined gathers with each chunk's column ids staged in shared memory by TMA
  *    bulk copy one chunk ahead, 7 (gather and gather+scatter) lane-row slabs: each
  *    lane combines whole rows in registers, rows of one size side by side, from the
- *    plan's slab layout (no shared memory); defaults 2, 2, 5;
+ *    plan's slab layout (no shared memory); defaults 2, 2, 5; "ogs.kernel.f32" and
+ *    "ogs.kernel.gather.f32" (-1..7, default -1 = as the two above) choose the
+ *    gather+scatter and gather kernels of 4-byte values separately;
  *  "ogs.slabs" (1 = plans created afterwards also hold the slab layouts kernel 7
  *    runs on, about 4 bytes per entry and per row of each walk; default 0: kernel
  *    7 then runs as kernel 2), "ogs.slab_seg_shift" (8..22, default 17: rows are

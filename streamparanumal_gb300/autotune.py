@@ -89,10 +89,12 @@ KNOBS = {"order": "ogs.order", "rows": "ogs.rows", "page_shift": "ogs.page_shift
          "kernel_gs": "ogs.kernel", "kernel_gather": "ogs.kernel.gather",
          "kernel_scatter": "ogs.kernel.scatter", "scatter_pages": "ogs.scatter_pages",
          "slabs": "ogs.slabs", "slab_seg_shift": "ogs.slab_seg_shift",
-         "slab_code_shift": "ogs.slab_code_shift"}
+         "slab_code_shift": "ogs.slab_code_shift", "kernel_gs32": "ogs.kernel.f32",
+         "kernel_gather32": "ogs.kernel.gather.f32"}
 # knobs a table entry may leave out: the library defaults
 PLAN_DEFAULTS = {"ball_shift": 0, "gs_order": -1, "scatter_pages": 1, "slabs": 0,
-                 "slab_seg_shift": SLAB_SEG_SHIFT, "slab_code_shift": 0}
+                 "slab_seg_shift": SLAB_SEG_SHIFT, "slab_code_shift": 0, "kernel_gs32": -1,
+                 "kernel_gather32": -1}
 
 
 def code_shift(p: int) -> int:
@@ -101,6 +103,8 @@ def code_shift(p: int) -> int:
     most 12 bits, p <= 15)."""
     return min(12, max(3, ((p + 1) ** 3 - 1).bit_length()))
 GS_WALK_KERNELS = (1, 2, 3, 5, 7)
+# the table keys of the operations whose 4-byte kernel is chosen on its own
+KEY32 = {"BS6": "kernel_gather32", "BS8": "kernel_gs32"}
 # FP64 times within this fraction of an operation's fastest count as a tie, broken
 # by the FP32 time (the storage form whose kernels differ most)
 FP32_TIE = 0.02
@@ -132,7 +136,8 @@ def _kernels(pc: dict, op: str) -> list[int]:
 def _slabs(choice: dict, p: int | None = None) -> dict:
     """A chosen configuration builds the slab layouts only when a kernel 7 uses them
     (with 16-bit member codes for degree p when p is given)."""
-    if 7 in (choice.get("kernel_gather"), choice.get("kernel_gs")):
+    if 7 in (choice.get("kernel_gather"), choice.get("kernel_gs"), choice.get("kernel_gather32"),
+             choice.get("kernel_gs32")):
         choice.update(slabs=1, slab_seg_shift=SLAB_SEG_SHIFT)
         if p is not None:
             choice["slab_code_shift"] = code_shift(p)
@@ -171,6 +176,15 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
                 win = min(near, key=lambda t: t[8])
             bnnz, k, ms = win[4], win[5], win[7]
             choice[key] = k
+            # 4-byte values may take another chunk kernel of this layout
+            c32 = [t for t in cands if len(t) > 8 and t[8] is not None and t[:4] == layout
+                   and t[5] >= 1]
+            if op in KEY32 and c32:
+                b32 = min(c32, key=lambda t: t[8])
+                own32 = win[8] if len(win) > 8 and win[8] is not None else None
+                # a kernel of its own only when it beats the FP64 choice by the tie band
+                if b32[5] != k and (own32 is None or b32[8] * (1.0 + FP32_TIE) < own32):
+                    choice[KEY32[op]] = b32[5]
             if op == "BS7" and k == 5:
                 choice["scatter_pages"] = int(win[:4] == layout and order >= 1)
             if k == 0 and (op != "BS8" or "block_nnz" not in choice):
@@ -262,6 +276,14 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                 go, gp, gb, k = win[2]
                 best.update(gs_order=go, gs_page_shift=gp, gs_ball_shift=gb, kernel_gs=k)
                 best_total += win[0] - best_gs_ms
+                # the 4-byte gather+scatter takes the fastest kernel on that walk
+                w32 = [t for t in walk_timings if t[:3] == (go, gp, gb) and t[5] is not None]
+                best.pop("kernel_gs32", None)
+                if w32:
+                    b32 = min(w32, key=lambda t: t[5])
+                    own32 = next((t[5] for t in w32 if t[3] == k), None)
+                    if b32[3] != k and (own32 is None or b32[5] * (1.0 + FP32_TIE) < own32):
+                        best["kernel_gs32"] = b32[3]
         _slabs(best, p)
     finally:
         _set(saved)

@@ -66,6 +66,8 @@ enum TuneKey : int {
   kTuneOgsSlabLoad,         // kernel 7: value loads 0 plain, 1 L2 only, 2 evict-first, 3 read-only path
   kTuneOgsSlabDefer,        // kernel 7 gather+scatter: 1 = a pass's stores after the next pass's loads
   kTuneOgsSlabCodeShift,    // ogs plan: 0 = 32-bit slab ids, 6..12 = 16-bit codes with that many low bits
+  kTuneOgsKernel32,         // ogs gather+scatter of 4-byte values: kernel variant, -1 = as ogs.kernel
+  kTuneOgsKernelGather32,   // ogs gather of 4-byte values: kernel variant, -1 = as ogs.kernel.gather
   kTuneCount
 };
 int64_t tune(TuneKey k);

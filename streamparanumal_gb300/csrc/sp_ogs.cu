@@ -924,6 +924,14 @@ static inline int variant(TuneKey key, int K, int32_t nchunks) {
   return (K == 1 && nchunks > 0) ? (int)tune(key) : 0;
 }
 
+// The same for 4-byte values, which may take a kernel of their own (knobs
+// ogs.kernel.f32 / ogs.kernel.gather.f32; -1 = as for 8-byte values).
+template <typename T>
+static inline int variant_for(TuneKey key, TuneKey key32, int K, int32_t nchunks) {
+  if (sizeof(T) == 4 && K == 1 && nchunks > 0 && tune(key32) >= 0) return (int)tune(key32);
+  return variant(key, K, nchunks);
+}
+
 // The arrays one warp-chunk launch walks: T chunks use the grouped rows when the
 // plan has them; N chunks always use CSR order.
 struct ChunkArgs {
@@ -1144,7 +1152,7 @@ template <typename T, int OP>
 static void launch_gs(const sp_ogs_plan* p, sp_transpose trans, int K, T* v, cudaStream_t s) {
   if (p->NrowBlocksT == 0) return;
   dim3 grid(p->NrowBlocksT, K);
-  const int kv = variant(kTuneOgsKernel, K, p->nchunksT);
+  const int kv = variant_for<T>(kTuneOgsKernel, kTuneOgsKernel32, K, p->nchunksT);
   if ((trans == SP_SYM || p->n_is_t) && kv > 0 && p->nchunksGS > 0) {
     launch_chunked_gather<T, OP, 0>(kv, chunks_gs(p), v, nullptr, s);  // 4 runs as 2 here
   } else if ((trans == SP_SYM || p->n_is_t) && kv > 0) {
@@ -1166,7 +1174,8 @@ template <typename T, int OP>
 static void launch_gather(const sp_ogs_plan* p, sp_transpose trans, int K, T* gv, const T* v,
                           cudaStream_t s) {
   const bool useN = (trans == SP_NOTRANS);
-  const int kv = variant(kTuneOgsKernelGather, K, useN ? p->nchunksN : p->nchunksT);
+  const int kv = variant_for<T>(kTuneOgsKernelGather, kTuneOgsKernelGather32, K,
+                                useN ? p->nchunksN : p->nchunksT);
   if (kv > 0) {
     launch_chunked_gather<T, OP, 1>(kv, useN ? chunks_n(p) : chunks_t(p), const_cast<T*>(v), gv,
                                     s);

@@ -63,7 +63,8 @@ def test_committed_table_is_well_formed():
         assert set(cfg) <= set(autotune.KNOBS)
         assert cfg["order"] in (0, 1, 2) and cfg["kernel_gs"] in (0, 1, 2, 3, 4, 5, 7)
         # the slab layouts are built exactly where a kernel 7 runs on them
-        uses = 7 in (cfg["kernel_gather"], cfg["kernel_gs"])
+        uses = 7 in (cfg["kernel_gather"], cfg["kernel_gs"], cfg.get("kernel_gather32"),
+                     cfg.get("kernel_gs32"))
         assert cfg.get("slabs", 0) == int(uses)
         p = int(key[1:].split("_")[0])
         assert cfg.get("slab_code_shift", 0) == (autotune.code_shift(p) if uses else 0)
@@ -158,7 +159,22 @@ def test_choose_breaks_near_ties_by_the_fp32_time():
          else x for x in t]
     best, _, _ = autotune.choose(t)
     assert best["kernel_gather"] == 7 and best["slabs"] == 1
-    # outside the tie band the FP64 time decides
+    # outside the tie band the FP64 time decides; FP32 keeps kernel 7 of its own
     t = [x[:7] + (0.52 if x[:7] == walk + (7, "BS6") else x[7], x[8]) for x in t]
     best, _, _ = autotune.choose(t)
-    assert best["kernel_gather"] == 2 and "slabs" not in best
+    assert best["kernel_gather"] == 2 and best["kernel_gather32"] == 7
+    assert best["slabs"] == 1
+
+
+def test_choose_takes_a_4byte_kernel_of_its_own():
+    walk = (1, 1, 9, 19, 2048)
+    t = [x + (1.0,) for x in _timings({walk + (2, "BS6"): 0.5, walk + (2, "BS8"): 0.5})]
+    # FP64 prefers kernel 2 by far; FP32 runs kernel 7 fastest on this layout
+    t = [x[:8] + (0.2,) if x[:7] in (walk + (7, "BS6"), walk + (7, "BS8")) else x for x in t]
+    best, _, _ = autotune.choose(t)
+    assert best["kernel_gather"] == 2 and best["kernel_gather32"] == 7
+    assert best["kernel_gs"] == 2 and best["kernel_gs32"] == 7 and best["slabs"] == 1
+    # no separate key when FP32's winner is the FP64 one
+    t = [x[:8] + (1.0,) for x in t]
+    best, _, _ = autotune.choose(t)
+    assert "kernel_gather32" not in best and "kernel_gs32" not in best

@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_order",
          "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.slabs", "ogs.slab_seg_shift",
          "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.slab_defer",
-         "ogs.slab_code_shift", "ogs.page_shift", "ogs.ball_shift")
+         "ogs.slab_code_shift", "ogs.kernel.f32", "ogs.kernel.gather.f32", "ogs.page_shift",
+         "ogs.ball_shift")
 
 
 @pytest.fixture
@@ -173,6 +174,31 @@ def test_slabs_with_16bit_codes(cuda, orc, knobs, box, shift, order, gs_order):
     np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
     for defer in (0, 1):
         knobs("ogs.slab_defer", defer)
+        dq = torch.from_numpy(q.copy()).cuda()
+        h.GatherScatter(dq, 1, O.Add, O.Sym)
+        np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+
+
+@pytest.mark.parametrize("k64,k32", [(2, 7), (7, 2), (7, -1)])
+def test_4byte_values_take_their_own_kernel(cuda, orc, knobs, k64, k32):
+    """ogs.kernel.f32 / ogs.kernel.gather.f32 pick the kernels of 4-byte values
+    apart from 8-byte ones; the bits do not change."""
+    knobs("ogs.order", 1)
+    knobs("ogs.slab_code_shift", 9)
+    ids = O.box_hex_ids(5, 4, 3, 7, 2024)
+    h, ref = make(orc, ids)
+    for key in ("ogs.kernel", "ogs.kernel.gather"):
+        knobs(key, k64)
+    for key in ("ogs.kernel.f32", "ogs.kernel.gather.f32"):
+        knobs(key, k32)
+    check_fp64(orc, h, ref, ids.size, 21)
+    rs, ci = ref["rsT"], ref["ciT"]
+    for dt, tdt in ((np.float32, torch.float32), (np.int32, torch.int32)):
+        q = orc.uniform(ids.size, 22).astype(np.float32)
+        q = q if dt == np.float32 else np.round(q * 1000).astype(np.int32)
+        gq = torch.zeros(rs.size - 1, dtype=tdt, device="cuda")
+        h.Gather(gq, torch.from_numpy(q).cuda(), 1, O.Add, O.Trans)
+        np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q))
         dq = torch.from_numpy(q.copy()).cuda()
         h.GatherScatter(dq, 1, O.Add, O.Sym)
         np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
