@@ -105,8 +105,7 @@ def code_shift(p: int) -> int:
 GS_WALK_KERNELS = (1, 2, 3, 5, 7)
 # the table keys of the operations whose 4-byte kernel is chosen on its own
 KEY32 = {"BS6": "kernel_gather32", "BS8": "kernel_gs32"}
-# FP64 times within this fraction of an operation's fastest count as a tie, broken
-# by the FP32 time (the storage form whose kernels differ most)
+# a 4-byte kernel of its own must beat the 8-byte choice's FP32 time by this much
 FP32_TIE = 0.02
 
 
@@ -154,9 +153,10 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
     gather+scatter may still get a walk of its own afterwards, which is built with
     the chosen layout's row grouping, so its time on the layout counts too).
     Returns (knobs, BS6 + BS7 ms, BS8 ms).  A candidate may carry a ninth field,
-    its time with FP32 values: among the kernels within FP32_TIE of the fastest
-    FP64 time of an operation, the one fastest in FP32 is taken (the FP64 time
-    still decides the layout)."""
+    its time with FP32 values: for BS6 and BS8 the chunk kernel of the chosen
+    layout fastest in FP32 becomes the 4-byte kernel (kernel_gather32 /
+    kernel_gs32) when it beats the FP64 choice's FP32 time by more than FP32_TIE;
+    the FP64 times alone decide the layout and the 8-byte kernels."""
     best_key, best, best_main, best_gs_ms = None, None, None, None
     for layout in sorted({t[:4] for t in timings}):
         order, rows, shift, ball = layout
@@ -170,10 +170,6 @@ def choose(timings: list[tuple]) -> tuple[dict, float, float]:
                 t[:4] == layout or t[5] == 0 or
                 (op == "BS7" and t[5] == 5 and t[0] == 0 and t[1] == 0))]
             win = min(cands, key=lambda t: t[7])
-            near = [t for t in cands if len(t) > 8 and t[8] is not None
-                    and t[7] <= win[7] * (1.0 + FP32_TIE)]
-            if len(near) > 1:
-                win = min(near, key=lambda t: t[8])
             bnnz, k, ms = win[4], win[5], win[7]
             choice[key] = k
             # 4-byte values may take another chunk kernel of this layout
@@ -261,17 +257,10 @@ def tune_ogs(E: int, p: int, perm_seed: int = 0, dtype=torch.float64, reps: int 
                 h.Free()
         best["gs_order"] = -1
         if walk_timings:
-            # the chosen layout's own gather+scatter against the walks, with the same
-            # FP32 tie-break as choose()
-            own = next((t for t in timings if t[:4] == (best["order"], best["rows"],
-                                                       best["page_shift"], best["ball_shift"])
-                        and t[6] == "BS8" and t[5] == best["kernel_gs"]), None)
+            # the chosen layout's own gather+scatter against the walks, by FP64 time
             cands = [(t[4], t[5], t[:4]) for t in walk_timings]
-            cands.append((best_gs_ms, own[8] if own is not None and len(own) > 8 else None, None))
+            cands.append((best_gs_ms, None, None))
             win = min(cands, key=lambda c: c[0])
-            near = [c for c in cands if c[1] is not None and c[0] <= win[0] * (1.0 + FP32_TIE)]
-            if len(near) > 1:
-                win = min(near, key=lambda c: c[1])
             if win[2] is not None:
                 go, gp, gb, k = win[2]
                 best.update(gs_order=go, gs_page_shift=gp, gs_ball_shift=gb, kernel_gs=k)

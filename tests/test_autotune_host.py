@@ -152,18 +152,18 @@ def test_code_shift_covers_an_element():
         assert (p + 1) ** 3 <= 1 << autotune.code_shift(p)
 
 
-def test_choose_breaks_near_ties_by_the_fp32_time():
+def test_choose_fp64_decides_the_8byte_kernel_fp32_its_own():
     walk = (1, 1, 9, 19, 2048)
     t = [x + (None,) for x in _timings({walk + (2, "BS6"): 0.500, walk + (7, "BS6"): 0.505})]
     t = [x[:8] + ((0.30 if x[5] == 7 else 0.40),) if x[:7] in (walk + (2, "BS6"), walk + (7, "BS6"))
          else x for x in t]
     best, _, _ = autotune.choose(t)
-    assert best["kernel_gather"] == 7 and best["slabs"] == 1
-    # outside the tie band the FP64 time decides; FP32 keeps kernel 7 of its own
-    t = [x[:7] + (0.52 if x[:7] == walk + (7, "BS6") else x[7], x[8]) for x in t]
+    assert best["kernel_gather"] == 2 and best["kernel_gather32"] == 7 and best["slabs"] == 1
+    # within the band FP32 keeps the 8-byte kernel
+    t = [x[:8] + ((0.395 if x[5] == 7 else 0.40),) if x[:7] in (walk + (2, "BS6"), walk + (7, "BS6"))
+         else x for x in t]
     best, _, _ = autotune.choose(t)
-    assert best["kernel_gather"] == 2 and best["kernel_gather32"] == 7
-    assert best["slabs"] == 1
+    assert best["kernel_gather"] == 2 and "kernel_gather32" not in best and "slabs" not in best
 
 
 def test_choose_takes_a_4byte_kernel_of_its_own():
