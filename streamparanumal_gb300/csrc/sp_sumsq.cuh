@@ -188,7 +188,7 @@ SP_SQ_HD void add(Acc& s, double a) {
   const uint32_t lo = (uint32_t)b, hi = (uint32_t)(b >> 32);
   const uint32_t t = s.e20 - (hi & kExpMask);  // (Emax - E) << 20, wraps when E > Emax
   if (t <= (kWin << 20)) add_window(s, lo, hi, t >> 19);
-  else add_outside(s, a, lo, hi, hi & kExpMask);
+  else if (((hi << 1) | lo) != 0u) add_outside(s, a, lo, hi, hi & kExpMask);  // +-0 adds nothing
 }
 
 // a += b: both aligned to the larger window top, then added as integers; the
