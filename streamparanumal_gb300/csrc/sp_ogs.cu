@@ -1460,6 +1460,9 @@ static sp_status build_slab_layout(sp_ogs_plan* p, const std::vector<int32_t>& q
   std::vector<int32_t> desc, ids, rows;
   build_slabs(quads, wrs, wci, perm, (int)tune(kTuneOgsSlabSegShift), with_rows, desc, ids,
               rows);
+  // The kernel addresses ids with 32-bit offsets; a walk whose padded slabs pass
+  // 2^31 - 1 words keeps no slabs and its launches run kernel 2.
+  if (ids.size() > (size_t)INT32_MAX) return SP_SUCCESS;
   sp_status st;
   if ((st = upload(desc, desc_out, s))) return st;
   if ((st = upload(ids, ids_out, s))) return st;
@@ -1480,7 +1483,6 @@ static sp_status build_slab_layout(sp_ogs_plan* p, const std::vector<int32_t>& q
         p->slab_coded_entries +=
             (int64_t)(((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255)) * desc[4 * g + 2];
       }
-    SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   }
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;

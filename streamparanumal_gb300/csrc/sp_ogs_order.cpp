@@ -17,6 +17,7 @@
 #include <parallel/algorithm>
 
 #include <algorithm>
+#include <cstdint>
 #include <vector>
 
 #include "sp_ogs_plan.h"
@@ -520,7 +521,7 @@ void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>
   const int32_t mask = (1 << shift) - 1;
   codes.assign(ids.size(), 0);
   tdesc.assign(2 * std::max<int64_t>(nslabs, 1), -1);
-  std::vector<int32_t> ntab(nslabs + 1, 0);
+  std::vector<int64_t> ntab(nslabs + 1, 0);
   // pass 1: the distinct high parts of each slab (first-appearance order), codes
 #pragma omp parallel
   {
@@ -547,7 +548,12 @@ void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>
     }
   }
   for (int64_t g = 0; g < nslabs; ++g) ntab[g + 1] += ntab[g];
-  tables.assign(std::max<int32_t>(ntab[nslabs], 1), 0);
+  if (ntab[nslabs] > INT32_MAX) {  // table offsets are 32-bit: leave every slab uncoded
+    for (int64_t g = 0; g < nslabs; ++g) tdesc[2 * g + 1] = 0;
+    tables.assign(1, 0);
+    return;
+  }
+  tables.assign(std::max<int64_t>(ntab[nslabs], 1), 0);
   // pass 2: the tables (high part << shift), and each compressed slab's offset
 #pragma omp parallel
   {
@@ -564,7 +570,7 @@ void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>
         if (std::find(tab.begin(), tab.end(), hi) == tab.end()) tab.push_back(hi);
       }
       for (size_t t = 0; t < tab.size(); ++t) tables[ntab[g] + t] = tab[t] << shift;
-      tdesc[2 * g] = ntab[g];
+      tdesc[2 * g] = (int32_t)ntab[g];
     }
   }
 }
