@@ -96,7 +96,11 @@ void        sp_launch_count_reset(void);
  *    (0..12, default 0: with s > 0 a slab whose ids have at most 128 distinct high
  *    parts id >> s stores them as 16-bit codes (table index << s | low s bits),
  *    which kernel 7 decodes through the slab's table; s = log2 of the nodes per
- *    element, e.g. 9 at p = 7, makes a high part an element);
+ *    element, e.g. 9 at p = 7, makes a high part an element), "ogs.slab_row_codes"
+ *    (0..1, default 0: with s > 0 the gather's slabs also hold the output row of
+ *    each of their rows as such a code, decoded through a second table per slab
+ *    of at most 32 runs by kernel 7's default Add gather; measured on GB300 +8 %
+ *    FP64 at p = 5 on permuted boxes, -4 % at p = 7 and -12 % for FP32, hence off);
  *  "ogs.slab_lane" (0..16, default 0: members in flight per lane and pass of
  *    kernel 7 -- 0 = 8, and 16 for the gather+scatter of 4-byte values, 1..8 = 8,
  *    9..16 = 16), "ogs.slab_ctas" (0..4, default 0: resident CTAs of 256
@@ -305,6 +309,7 @@ typedef struct {
   int32_t NslabsGS;   /* lane-row slabs of the gather+scatter walk (0: none)         */
   int32_t slabCodeShift;    /* low bits of the slabs' 16-bit member codes (0: none)  */
   int64_t slabCodedEntries; /* entries of both walks' slabs held as 16-bit codes      */
+  int64_t slabCodedRows;    /* gather rows whose row word is held as a 16-bit code     */
 } sp_ogs_info;
 
 /* Build from global ids (ogs_t::Setup, include/ogs.hpp:221-228 at one rank):

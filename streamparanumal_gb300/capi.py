@@ -50,7 +50,8 @@ class OgsInfo(ctypes.Structure):
                 ("NchunksN", c_int32), ("chunkOrder", c_int32), ("rowOrder", c_int32),
                 ("NchunksGS", c_int32), ("gsRowOrder", c_int32), ("NpagesT", c_int32),
                 ("pageShift", c_int32), ("waitErrors", c_int32), ("NslabsT", c_int32),
-                ("NslabsGS", c_int32), ("slabCodeShift", c_int32), ("slabCodedEntries", c_int64)]
+                ("NslabsGS", c_int32), ("slabCodeShift", c_int32), ("slabCodedEntries", c_int64),
+                ("slabCodedRows", c_int64)]
 
 
 class MrInfo(ctypes.Structure):

@@ -68,6 +68,7 @@ enum TuneKey : int {
   kTuneOgsSlabCodeShift,    // ogs plan: 0 = 32-bit slab ids, 6..12 = 16-bit codes with that many low bits
   kTuneOgsKernel32,         // ogs gather+scatter of 4-byte values: kernel variant, -1 = as ogs.kernel
   kTuneOgsKernelGather32,   // ogs gather of 4-byte values: kernel variant, -1 = as ogs.kernel.gather
+  kTuneOgsSlabRowCodes,     // ogs plan: 1 = with member codes, the gather slabs' row words coded too (default 0)
   kTuneCount
 };
 int64_t tune(TuneKey k);

@@ -957,7 +957,9 @@ static inline ChunkArgs chunks_t(const sp_ogs_plan* p) {
                    g ? reinterpret_cast<const int2*>(p->d_singT) : nullptr,
                    SlabArgs{reinterpret_cast<const int4*>(p->d_slabsT), p->nslabsT, p->d_slabIdsT,
                             p->d_slabRowsT, p->d_slabCodesT, p->d_slabTabsT,
-                            reinterpret_cast<const int2*>(p->d_slabTdT), p->slab_code_shift}};
+                            reinterpret_cast<const int2*>(p->d_slabTdT), p->slab_code_shift,
+                            p->d_slabRowCodesT, p->d_slabRowTabsT,
+                            reinterpret_cast<const int2*>(p->d_slabRowTdT)}};
 }
 // The gather+scatter walk when the plan has one (kernel 4 needs the column-order
 // arrays of the main walk, so it runs as kernel 2 there).
@@ -969,12 +971,14 @@ static inline ChunkArgs chunks_gs(const sp_ogs_plan* p) {
                    p->gs_grouped ? reinterpret_cast<const int2*>(p->d_singGS) : nullptr,
                    SlabArgs{reinterpret_cast<const int4*>(p->d_slabsGS), p->nslabsGS,
                             p->d_slabIdsGS, nullptr, p->d_slabCodesGS, p->d_slabTabsGS,
-                            reinterpret_cast<const int2*>(p->d_slabTdGS), p->slab_code_shift}};
+                            reinterpret_cast<const int2*>(p->d_slabTdGS), p->slab_code_shift,
+                            nullptr, nullptr, nullptr}};
 }
 static inline ChunkArgs chunks_n(const sp_ogs_plan* p) {
   return ChunkArgs{reinterpret_cast<const int4*>(p->d_chunksN), p->nchunksN, p->d_rowStartsNpad,
                    p->d_colIdsN, 0, nullptr, nullptr, nullptr, p->d_waitErr, nullptr,
-                   SlabArgs{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0}};
+                   SlabArgs{nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr,
+                            nullptr, nullptr}};
 }
 
 // Kernel 6: the pipelined persistent gathers of kernel 2 with the chunks' column ids
@@ -1383,6 +1387,12 @@ static void free_plan_device(sp_ogs_plan* p) {
   for (int32_t* q : {p->d_slabsT, p->d_slabIdsT, p->d_slabRowsT, p->d_slabsGS, p->d_slabIdsGS,
                      p->d_slabTabsT, p->d_slabTdT, p->d_slabTabsGS, p->d_slabTdGS})
     if (q) cudaFree(q);
+  for (int32_t* q : {p->d_slabRowTabsT, p->d_slabRowTdT})
+    if (q) cudaFree(q);
+  if (p->d_slabRowCodesT) cudaFree(p->d_slabRowCodesT);
+  p->d_slabRowCodesT = nullptr;
+  p->d_slabRowTabsT = p->d_slabRowTdT = nullptr;
+  p->slab_coded_rows = 0;
   for (uint16_t* q : {p->d_slabCodesT, p->d_slabCodesGS})
     if (q) cudaFree(q);
   p->d_slabsT = p->d_slabIdsT = p->d_slabRowsT = p->d_slabsGS = p->d_slabIdsGS = nullptr;
@@ -1451,7 +1461,8 @@ static std::vector<int32_t> singleton_split(const std::vector<int32_t>& quads,
 
 // Slab layout of one walk (build_slabs), uploaded; `rows_out` null for a walk that
 // only serves the in-place gather+scatter.  With ogs.slab_code_shift > 0 also the
-// 16-bit codes of the slabs that compress (compress_slabs).
+// 16-bit codes of the slabs that compress (compress_slabs) and, for a gather walk
+// with ogs.slab_row_codes, those of its row words (compress_slab_rows).
 static sp_status build_slab_layout(sp_ogs_plan* p, const std::vector<int32_t>& quads,
                                    const int32_t* wrs, const int32_t* wci, const int32_t* perm,
                                    bool with_rows, int32_t** desc_out, int32_t** ids_out,
@@ -1483,6 +1494,20 @@ static sp_status build_slab_layout(sp_ogs_plan* p, const std::vector<int32_t>& q
         p->slab_coded_entries +=
             (int64_t)(((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255)) * desc[4 * g + 2];
       }
+    if (with_rows && tune(kTuneOgsSlabRowCodes) == 1) {
+      std::vector<uint16_t> rcodes;
+      std::vector<int32_t> rtabs, rtd;
+      compress_slab_rows(desc, rows, shift, rcodes, rtabs, rtd);
+      if ((st = upload(rcodes, &p->d_slabRowCodesT, s))) return st;
+      if ((st = upload(rtabs, &p->d_slabRowTabsT, s))) return st;
+      if ((st = upload(rtd, &p->d_slabRowTdT, s))) return st;
+      for (int32_t g = 0; g < *nslabs; ++g)
+        if (rtd[2 * g + 1] > 0) {
+          const int32_t w = desc[4 * g + 3];
+          p->slab_coded_rows += (int64_t)((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255);
+        }
+      SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
+    }
   }
   SP_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die with this scope
   return SP_SUCCESS;
@@ -1836,6 +1861,7 @@ sp_status sp_ogs_plan_info(const sp_ogs_plan* p, sp_ogs_info* info) {
   info->NslabsGS = p->nslabsGS;
   info->slabCodeShift = p->slab_code_shift;
   info->slabCodedEntries = p->slab_coded_entries;
+  info->slabCodedRows = p->slab_coded_rows;
   info->waitErrors = 0;
   if (p->d_waitErr) {
     int32_t* dev = p->d_waitErr;

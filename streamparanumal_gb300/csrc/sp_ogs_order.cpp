@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "sp_ogs_plan.h"
@@ -513,13 +514,18 @@ void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int
   }
 }
 
-void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>& ids, int shift,
-                    std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
-                    std::vector<int32_t>& tdesc) {
-  const int64_t nslabs = (int64_t)desc.size() / 4;
-  const int32_t maxTab = std::min<int32_t>(kSlabCodeTable, 1 << (16 - shift));
+// 16-bit codes of the words of every slab g, words[first(g) .. first(g) + count(g))
+// (compress_slabs, compress_slab_rows): a slab whose words have at most
+// min(tableCap, 2^(16 - shift)) distinct high parts w >> shift gets a table of them
+// (first-appearance order) and its words as (table index << shift | low bits); the
+// others keep their 32-bit words.
+template <typename Span>
+static void code_slab_words(int64_t nslabs, Span span, const std::vector<int32_t>& words,
+                            int shift, int32_t tableCap, std::vector<uint16_t>& codes,
+                            std::vector<int32_t>& tables, std::vector<int32_t>& tdesc) {
+  const int32_t maxTab = std::min<int32_t>(tableCap, 1 << (16 - shift));
   const int32_t mask = (1 << shift) - 1;
-  codes.assign(ids.size(), 0);
+  codes.assign(words.size(), 0);
   tdesc.assign(2 * std::max<int64_t>(nslabs, 1), -1);
   std::vector<int64_t> ntab(nslabs + 1, 0);
   // pass 1: the distinct high parts of each slab (first-appearance order), codes
@@ -528,20 +534,18 @@ void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>
     std::vector<int32_t> tab;
 #pragma omp for schedule(dynamic, 64)
     for (int64_t g = 0; g < nslabs; ++g) {
-      const int32_t E = desc[4 * g], m = desc[4 * g + 2], w = desc[4 * g + 3];
-      const int32_t nl = w & 255, rem = (w >> 8) & 255, Re = w >> 16;
-      const int64_t n = (int64_t)((Re - 1) * nl + rem) * m;
+      const std::pair<int64_t, int64_t> fc = span(g);
       tab.clear();
-      bool ok = m > 0;
-      for (int64_t k = 0; k < n && ok; ++k) {
-        const int32_t hi = ids[E + k] >> shift;
+      bool ok = fc.second > 0;
+      for (int64_t k = 0; k < fc.second && ok; ++k) {
+        const int32_t word = words[fc.first + k], hi = word >> shift;
         int32_t t = 0;
         while (t < (int32_t)tab.size() && tab[t] != hi) ++t;
         if (t == (int32_t)tab.size()) {
           if ((int32_t)tab.size() == maxTab) ok = false;
           else tab.push_back(hi);
         }
-        if (ok) codes[E + k] = (uint16_t)((t << shift) | (ids[E + k] & mask));
+        if (ok) codes[fc.first + k] = (uint16_t)((t << shift) | (word & mask));
       }
       ntab[g + 1] = ok ? (int32_t)tab.size() : 0;
       tdesc[2 * g + 1] = ok ? (int32_t)tab.size() : 0;
@@ -561,18 +565,42 @@ void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>
 #pragma omp for schedule(dynamic, 64)
     for (int64_t g = 0; g < nslabs; ++g) {
       if (tdesc[2 * g + 1] == 0) continue;
-      const int32_t E = desc[4 * g], m = desc[4 * g + 2], w = desc[4 * g + 3];
-      const int32_t nl = w & 255, rem = (w >> 8) & 255, Re = w >> 16;
-      const int64_t n = (int64_t)((Re - 1) * nl + rem) * m;
+      const std::pair<int64_t, int64_t> fc = span(g);
       tab.clear();
-      for (int64_t k = 0; k < n; ++k) {
-        const int32_t hi = ids[E + k] >> shift;
+      for (int64_t k = 0; k < fc.second; ++k) {
+        const int32_t hi = words[fc.first + k] >> shift;
         if (std::find(tab.begin(), tab.end(), hi) == tab.end()) tab.push_back(hi);
       }
       for (size_t t = 0; t < tab.size(); ++t) tables[ntab[g] + t] = tab[t] << shift;
       tdesc[2 * g] = (int32_t)ntab[g];
     }
   }
+}
+
+// Rows of slab g: n = (Re - 1) * nl + rem.
+static inline int64_t slab_nrows(const std::vector<int32_t>& desc, int64_t g) {
+  const int32_t w = desc[4 * g + 3];
+  return (int64_t)((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255);
+}
+
+void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>& ids, int shift,
+                    std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
+                    std::vector<int32_t>& tdesc) {
+  code_slab_words(
+      (int64_t)desc.size() / 4,
+      [&](int64_t g) {
+        return std::make_pair((int64_t)desc[4 * g], slab_nrows(desc, g) * desc[4 * g + 2]);
+      },
+      ids, shift, kSlabCodeTable, codes, tables, tdesc);
+}
+
+void compress_slab_rows(const std::vector<int32_t>& desc, const std::vector<int32_t>& rows,
+                        int shift, std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
+                        std::vector<int32_t>& tdesc) {
+  code_slab_words(
+      (int64_t)desc.size() / 4,
+      [&](int64_t g) { return std::make_pair((int64_t)desc[4 * g + 1], slab_nrows(desc, g)); },
+      rows, shift, kSlabRowTable, codes, tables, tdesc);
 }
 
 }  // namespace sp

@@ -114,6 +114,16 @@ constexpr int32_t kSlabCodeTable = 128;
 void compress_slabs(const std::vector<int32_t>& desc, const std::vector<int32_t>& ids, int shift,
                     std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
                     std::vector<int32_t>& tdesc);
+// The same codes for the row words of a gather walk's slabs (rows[first .. first +
+// n) of slab g, n its rows), at their own positions in `codes`, with a table per
+// slab of at most kSlabRowTable high parts (ogs.slab_row_codes).  The reference's
+// first-appearance row order numbers the rows that first appear in one element
+// consecutively, so a slab's rows, drawn from a few neighbouring elements, fall
+// into a few runs (on hex boxes of p = 1..15 at most 32 for 93-100 % of the slabs).
+constexpr int32_t kSlabRowTable = 32;
+void compress_slab_rows(const std::vector<int32_t>& desc, const std::vector<int32_t>& rows,
+                        int shift, std::vector<uint16_t>& codes, std::vector<int32_t>& tables,
+                        std::vector<int32_t>& tdesc);
 void build_slabs(const std::vector<int32_t>& quads, const int32_t* rs, const int32_t* ci,
                  const int32_t* perm, int seg_shift, bool with_rows, std::vector<int32_t>& desc,
                  std::vector<int32_t>& ids, std::vector<int32_t>& rows);
@@ -215,6 +225,12 @@ struct sp_ogs_plan {
   int32_t* d_slabTdGS = nullptr;
   int32_t slab_code_shift = 0;
   int64_t slab_coded_entries = 0;   // entries in compressed slabs, both walks
+  // the main walk's row words as 16-bit codes (compress_slab_rows; null unless
+  // ogs.slab_row_codes with a code shift)
+  uint16_t* d_slabRowCodesT = nullptr;
+  int32_t* d_slabRowTabsT = nullptr;
+  int32_t* d_slabRowTdT = nullptr;
+  int64_t slab_coded_rows = 0;
   // count of bounded device waits that gave up (the bulk-staged gathers' waits)
   int32_t* d_waitErr = nullptr;
   bool own_n_csr = false;         // d_rowStartsNpad / d_colIdsN are separate allocations

@@ -262,13 +262,23 @@ __device__ __forceinline__ void load_raw(const int32_t* __restrict__ ids,
 // pass's value loads.  With `codes` (ogs.slab_code_shift > 0) the slabs that
 // compressed read 16-bit member codes, decoded through their table of high parts,
 // which the warp keeps in shared memory (loaded one slab ahead into registers,
-// stored when the slab begins); the other slabs read their 32-bit ids.
-template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
+// stored when the slab begins); the other slabs read their 32-bit ids.  With
+// RC = 1 (gathers with `rcodes`, ogs.slab_row_codes): the full passes of a slab
+// whose row words compressed read 16-bit row codes likewise, decoded through the
+// slab's row table (at most 32 entries, one per lane), which is prefetched and
+// stored with the id table.  With RC = 0 the row words are the 32-bit ones, which
+// every plan keeps.
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0, int RC = 0>
 __global__ void __launch_bounds__(kOgsThreads, CTAS)
 k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __restrict__ ids,
               const int32_t* __restrict__ rows, T* v, T* gv, const uint16_t* __restrict__ codes,
-              const int32_t* __restrict__ tabs, const int2* __restrict__ td, int sh) {
+              const int32_t* __restrict__ tabs, const int2* __restrict__ td, int sh,
+              const uint16_t* __restrict__ rcodes, const int32_t* __restrict__ rtabs,
+              const int2* __restrict__ rtd) {
   __shared__ int32_t stab[kWarpsPerCta][kSlabCodeTable];
+  constexpr bool rcx = RC != 0 && MODE == 1;
+  __shared__ int32_t rstab[kWarpsPerCta][rcx ? kSlabRowTable : 1];
+  static_assert(kSlabRowTable <= 32, "a row table is one word per lane");
   constexpr bool defer = DF != 0 && MODE == 0;
   constexpr int TPL = kSlabCodeTable / 32;  // table words per lane
   T pval[KB];
@@ -285,6 +295,9 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
   int4 dn = (s + W < nslabs) ? __ldg(slabs + s + W) : zero;
   int2 t = codes ? __ldg(td + s) : plain;
   int2 tn = (codes && s + W < nslabs) ? __ldg(td + s + W) : plain;
+  const bool rc = rcx && rcodes != nullptr;
+  int2 rt = rc ? __ldg(rtd + s) : plain;
+  int2 rtn = (rc && s + W < nslabs) ? __ldg(rtd + s + W) : plain;
   int j0 = 0;
   bool full = pass_full<KB>(d, 0);
   int32_t raw[KB];
@@ -294,8 +307,9 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
 #pragma unroll
       for (int i = 0; i < TPL; ++i)
         if (lane + 32 * i < t.y) stab[w][lane + 32 * i] = __ldg(tabs + t.x + lane + 32 * i);
-      __syncwarp();
     }
+    if (rcx && rt.y > 0 && lane < rt.y) rstab[w][lane] = __ldg(rtabs + rt.x + lane);
+    if (t.y > 0 || (rcx && rt.y > 0)) __syncwarp();
   }
   while (true) {
     const int m = d.z, Re = d.w >> 16;
@@ -309,6 +323,7 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
     const bool fullx = has_next && pass_full<KB>(dx, jx);
     int32_t nraw[KB];
     int32_t ntab[TPL];
+    int32_t nrt = 0;  // this lane's word of the next slab's row table
     if (full) {
       int32_t cid[KB];
       if (t.y > 0) {
@@ -320,13 +335,21 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
       }
       T val[KB];
       int32_t rw[KB];
+      const bool rcoded = rcx && rt.y > 0;  // this slab's row words are codes
 #pragma unroll
       for (int u = 0; u < KB; ++u) val[u] = load_val<LD, MODE>(v + cid[u]);
       if (MODE == 1) {
-        const int32_t* rsrc = rows + d.y + j0 * 32 + lane;
+        if (rcoded) {
+          const uint16_t* rsrc = rcodes + d.y + j0 * 32 + lane;
 #pragma unroll
-        for (int jj = 0; jj < KB; ++jj)
-          if (jj < P) rw[jj] = __ldg(rsrc + 32 * jj);
+          for (int jj = 0; jj < KB; ++jj)
+            if (jj < P) rw[jj] = (int32_t)__ldg(rsrc + 32 * jj);
+        } else {
+          const int32_t* rsrc = rows + d.y + j0 * 32 + lane;
+#pragma unroll
+          for (int jj = 0; jj < KB; ++jj)
+            if (jj < P) rw[jj] = __ldg(rsrc + 32 * jj);
+        }
       }
       if (fullx) {
         load_raw<KB>(ids, codes, dx, jx, tx.y > 0, lane, nraw);
@@ -335,6 +358,12 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
           for (int i = 0; i < TPL; ++i)
             if (lane + 32 * i < tx.y) ntab[i] = __ldg(tabs + tx.x + lane + 32 * i);
         }
+        if (rcx && next_slab && lane < rtn.y) nrt = __ldg(rtabs + rtn.x + lane);
+      }
+      if (rcoded) {
+#pragma unroll
+        for (int jj = 0; jj < KB; ++jj)
+          if (jj < P) rw[jj] = rstab[w][rw[jj] >> sh] | (rw[jj] & mask);
       }
       if constexpr (defer) {
         flush_deferred<T, KB>(v, pval, pcid, pm);
@@ -362,6 +391,7 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
           for (int i = 0; i < TPL; ++i)
             if (lane + 32 * i < tx.y) ntab[i] = __ldg(tabs + tx.x + lane + 32 * i);
         }
+        if (rcx && next_slab && lane < rtn.y) nrt = __ldg(rtabs + rtn.x + lane);
       }
     }
     if (!has_next) break;
@@ -369,19 +399,26 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
       s += W;
       d = dn;
       t = tn;
+      rt = rtn;
       dn = (s + W < nslabs) ? __ldg(slabs + s + W) : zero;
       tn = (codes && s + W < nslabs) ? __ldg(td + s + W) : plain;
+      rtn = (rc && s + W < nslabs) ? __ldg(rtd + s + W) : plain;
     }
     j0 = jx;
     full = fullx;
     if (full) {
 #pragma unroll
       for (int u = 0; u < KB; ++u) raw[u] = nraw[u];
-      if (next_slab && t.y > 0) {
-        __syncwarp();  // every lane has decoded its last pass against the old table
+      const bool id_tab = next_slab && t.y > 0;
+      const bool row_tab = rcx && next_slab && rt.y > 0;
+      if (id_tab || row_tab) {
+        __syncwarp();  // every lane has decoded its last pass against the old tables
+        if (id_tab) {
 #pragma unroll
-        for (int i = 0; i < TPL; ++i)
-          if (lane + 32 * i < t.y) stab[w][lane + 32 * i] = ntab[i];
+          for (int i = 0; i < TPL; ++i)
+            if (lane + 32 * i < t.y) stab[w][lane + 32 * i] = ntab[i];
+        }
+        if (row_tab && lane < rt.y) rstab[w][lane] = nrt;
         __syncwarp();
       }
     }
@@ -389,15 +426,16 @@ k_ogsl_gather(const int4* __restrict__ slabs, int32_t nslabs, const int32_t* __r
   if constexpr (defer) flush_deferred<T, KB>(v, pval, pcid, pm);
 }
 
-template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0>
+template <typename T, int OP, int MODE, int KB, int CTAS, int LD = 0, int DF = 0, int RC = 0>
 static void launch_shape(const SlabArgs& a, T* v, T* gv, cudaStream_t s) {
   const int4* slabs = a.slabs;
   const int32_t nslabs = a.nslabs;
   const int64_t want = ((int64_t)nslabs + kWarpsPerCta - 1) / kWarpsPerCta;
   const int64_t cap = (int64_t)sm_count() * CTAS;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min(want, cap));
-  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD, DF><<<g, kOgsThreads, 0, s>>>(
-      slabs, nslabs, a.ids, a.rows, v, gv, a.codes, a.tabs, a.td, a.shift);
+  k_ogsl_gather<T, OP, MODE, KB, CTAS, LD, DF, RC><<<g, kOgsThreads, 0, s>>>(
+      slabs, nslabs, a.ids, a.rows, v, gv, a.codes, a.tabs, a.td, a.shift, a.rcodes, a.rtabs,
+      a.rtd);
 }
 
 // One pass size with the resident CTAs the knob ogs.slab_ctas asks for (Add only;
@@ -424,6 +462,11 @@ static void launch_ctas(const SlabArgs& a, T* v, T* gv, cudaStream_t s) {
       case 4: return launch_shape<T, OP, MODE, KB, 4>(a, v, gv, s);
       default: break;
     }
+  }
+  // row codes (plans built with ogs.slab_row_codes): the gather's default shape
+  // decodes them; every other shape reads the 32-bit row words
+  if constexpr (OP == SP_OP_ADD && MODE == 1 && KB == 8) {
+    if (a.rcodes) return launch_shape<T, OP, MODE, KB, dflt, 0, 0, 1>(a, v, gv, s);
   }
   launch_shape<T, OP, MODE, KB, dflt>(a, v, gv, s);
 }

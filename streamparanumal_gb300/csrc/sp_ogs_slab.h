@@ -7,7 +7,8 @@
 namespace sp {
 
 // The slab layout of one walk on the device (build_slabs; codes, tabs and td from
-// compress_slabs, or null with shift 0).
+// compress_slabs, or null with shift 0; rcodes, rtabs and rtd the row words' codes
+// from compress_slab_rows, or null).
 struct SlabArgs {
   const int4* slabs;
   int32_t nslabs;
@@ -17,6 +18,9 @@ struct SlabArgs {
   const int32_t* tabs;
   const int2* td;
   int shift;
+  const uint16_t* rcodes;
+  const int32_t* rtabs;
+  const int2* rtd;
 };
 
 // One launch over the slabs of a walk: MODE 1 gathers gv[row] = op over the row's

@@ -60,6 +60,7 @@ static TuneEntry g_tune[kTuneCount] = {
     {"ogs.slab_code_shift", 0, 12, {0}},
     {"ogs.kernel.f32", -1, 7, {-1}},
     {"ogs.kernel.gather.f32", -1, 7, {-1}},
+    {"ogs.slab_row_codes", 0, 1, {0}},
 };
 
 int64_t tune(TuneKey k) { return g_tune[k].value.load(std::memory_order_relaxed); }

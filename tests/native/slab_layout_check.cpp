@@ -2,9 +2,9 @@
 // index arithmetic of kernel 7 (streamparanumal_gb300/csrc/sp_ogs_slab.cu), with no
 // GPU: every slab's passes are walked as the kernel walks them -- full passes of KB
 // members per lane at 32-word strides, the general row steps of a slab's rest, the
-// any-size path, 16-bit codes decoded through the slab's table -- every index is
-// checked against its array, and the gather and in-place gather+scatter they imply
-// are compared bit for bit with the CSR-order sums.
+// any-size path, 16-bit member codes and row codes decoded through the slab's
+// tables -- every index is checked against its array, and the gather and in-place
+// gather+scatter they imply are compared bit for bit with the CSR-order sums.
 //
 // usage: slab_layout_check rs.bin ci.bin N order page_shift ball_shift seg_shift code_shift
 #include <cstdio>
@@ -41,8 +41,8 @@ static std::vector<int32_t> read_ints(const char* path) {
 }
 
 struct Layout {
-  std::vector<int32_t> desc, ids, rows, tabs, td;
-  std::vector<uint16_t> codes;
+  std::vector<int32_t> desc, ids, rows, tabs, td, rtabs, rtd;
+  std::vector<uint16_t> codes, rcodes;
   int shift = 0;
 };
 
@@ -66,6 +66,23 @@ static int32_t row_word(const Layout& L, bool gather, int64_t pos) {
   CHECK(pos >= 0 && pos < (int64_t)L.rows.size(), "row word %lld outside %zu", (long long)pos,
         L.rows.size());
   return (pos >= 0 && pos < (int64_t)L.rows.size()) ? L.rows[pos] : 0;
+}
+
+// The row word of a full pass, as the kernel reads it: a row code decoded through
+// the slab's row table (one word per lane) when the slab's rows compressed.
+static int32_t pass_row_word(const Layout& L, bool gather, int64_t g, int64_t pos) {
+  if (!gather || L.rtd.empty() || L.rtd[2 * g + 1] == 0) return row_word(L, gather, pos);
+  CHECK(pos >= 0 && pos < (int64_t)L.rcodes.size(), "row code %lld outside %zu",
+        (long long)pos, L.rcodes.size());
+  if (pos < 0 || pos >= (int64_t)L.rcodes.size()) return 0;
+  const int32_t c = L.rcodes[pos], t = c >> L.shift;
+  CHECK(t < L.rtd[2 * g + 1] && L.rtd[2 * g + 1] <= kSlabRowTable, "row table index %d of %d", t,
+        L.rtd[2 * g + 1]);
+  const int64_t at = (int64_t)L.rtd[2 * g] + t;
+  CHECK(at >= 0 && at < (int64_t)L.rtabs.size(), "row table word %lld", (long long)at);
+  const int32_t r = L.rtabs[at] | (c & ((1 << L.shift) - 1));
+  CHECK(r == L.rows[pos], "row code decodes to %d, row %d", r, L.rows[pos]);
+  return r;
 }
 
 struct Sink {
@@ -108,7 +125,8 @@ static void walk(const Layout& L, int KB, Sink& sink) {
           for (int jj = 0; jj < P; ++jj) {
             std::vector<int32_t> cols;
             for (int t = 0; t < m; ++t) cols.push_back(member(L, g, src + 32 * (jj * m + t)));
-            sink.row(row_word(L, sink.gather, (int64_t)rb + (int64_t)(j0 + jj) * 32 + lane), cols);
+            sink.row(pass_row_word(L, sink.gather, g, (int64_t)rb + (int64_t)(j0 + jj) * 32 + lane),
+                     cols);
           }
         }
     }
@@ -156,13 +174,20 @@ int main(int argc, char** argv) {
     want_g[r] = acc;
     for (int32_t i = rs[r]; i < rs[r + 1]; ++i) want_gs[ci[i]] = acc;
   }
-  long coded = 0, total = 0;
+  long coded = 0, total = 0, rows_coded = 0;
   for (int gather = 0; gather < 2; ++gather) {
     Layout L;
     build_slabs(quads, rs.data(), ci.data(), nullptr, seg, gather == 1, L.desc, L.ids, L.rows);
     if (shift > 0) {
       compress_slabs(L.desc, L.ids, shift, L.codes, L.tabs, L.td);
       L.shift = shift;
+      if (gather) {
+        compress_slab_rows(L.desc, L.rows, shift, L.rcodes, L.rtabs, L.rtd);
+        for (size_t g = 0; g < L.desc.size() / 4; ++g) {
+          const int32_t w = L.desc[4 * g + 3];
+          if (L.rtd[2 * g + 1] > 0) rows_coded += ((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255);
+        }
+      }
       for (size_t g = 0; g < L.desc.size() / 4; ++g) {
         const int32_t w = L.desc[4 * g + 3];
         const int64_t n = (int64_t)(((w >> 16) - 1) * (w & 255) + ((w >> 8) & 255)) * L.desc[4 * g + 2];
@@ -184,6 +209,7 @@ int main(int argc, char** argv) {
       }
     }
   }
-  std::printf("%s coded %ld of %ld\n", g_bad ? "FAILED" : "ok", coded, total);
+  std::printf("%s coded %ld of %ld rows %ld of %d\n", g_bad ? "FAILED" : "ok", coded, total,
+              rows_coded, nrows);
   return g_bad ? 1 : 0;
 }

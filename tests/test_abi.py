@@ -124,7 +124,8 @@ KNOB_RANGES = {  # key: (lowest, highest, default), as include/sp_capi.h documen
     "ogs.singles": (0, 2, 2), "reduce.rdotr_exact": (0, 1, 0), "ogs.slabs": (0, 1, 0), "ogs.slab_seg_shift": (8, 22, 17),
     "ogs.slab_lane": (0, 16, 0), "ogs.slab_ctas": (0, 4, 0),
     "ogs.slab_load": (0, 3, 0), "ogs.slab_defer": (0, 1, 1),
-    "ogs.slab_code_shift": (0, 12, 0), "ogs.kernel.f32": (-1, 7, -1),
+    "ogs.slab_code_shift": (0, 12, 0), "ogs.slab_row_codes": (0, 1, 0),
+    "ogs.kernel.f32": (-1, 7, -1),
     "ogs.kernel.gather.f32": (-1, 7, -1)}
 
 

@@ -18,7 +18,7 @@ KNOBS = ("ogs.kernel", "ogs.kernel.gather", "ogs.order", "ogs.rows", "ogs.gs_ord
          "ogs.gs_page_shift", "ogs.gs_ball_shift", "ogs.slabs", "ogs.slab_seg_shift",
          "ogs.slab_lane", "ogs.slab_ctas", "ogs.slab_load", "ogs.slab_defer",
          "ogs.slab_code_shift", "ogs.kernel.f32", "ogs.kernel.gather.f32", "ogs.page_shift",
-         "ogs.ball_shift")
+         "ogs.ball_shift", "ogs.slab_row_codes")
 
 
 @pytest.fixture
@@ -81,15 +81,20 @@ def test_slabs_fp64_every_walk(cuda, orc, knobs, box, order, rows, gs_order):
 
 @pytest.mark.parametrize("seg", [8, 10, 22])
 @pytest.mark.parametrize("lane", [0, 8, 16])
-def test_slab_segments_and_kernel_shapes(cuda, orc, knobs, seg, lane):
+@pytest.mark.parametrize("shift", [0, 8])
+def test_slab_segments_and_kernel_shapes(cuda, orc, knobs, seg, lane, shift):
     """Small segments leave many partial slabs (their last row step partly filled,
     steps of fewer than 32 lanes) between full passes; 8 or 16 members in flight
-    per lane, for FP64 and FP32, give the same bits."""
+    per lane, for FP64 and FP32, with 32-bit words or member and row codes, give
+    the same bits."""
     knobs("ogs.slab_seg_shift", seg)
     knobs("ogs.slab_lane", lane)
+    knobs("ogs.slab_code_shift", shift)
+    knobs("ogs.slab_row_codes", 1)
     knobs("ogs.order", 1)
     ids = O.box_hex_ids(6, 5, 4, 5, 2024)
     h, ref = make(orc, ids)
+    assert (h.info.slabCodedRows > 0) == (shift > 0)
     check_fp64(orc, h, ref, ids.size, 7)
     rs, ci = ref["rsT"], ref["ciT"]
     q = orc.uniform(ids.size, 8).astype(np.float32)
@@ -103,10 +108,14 @@ def test_slab_segments_and_kernel_shapes(cuda, orc, knobs, seg, lane):
 
 @pytest.mark.parametrize("load", [1, 2, 3])
 @pytest.mark.parametrize("ctas", [1, 3, 4])
-def test_slab_load_paths_and_ctas(cuda, orc, knobs, load, ctas):
+@pytest.mark.parametrize("shift", [0, 9])
+def test_slab_load_paths_and_ctas(cuda, orc, knobs, load, ctas, shift):
     """The value-load variants (L2 only, evict-first, read-only path) and the
-    resident-CTA shapes of kernel 7 give the same bits, FP64 and FP32."""
+    resident-CTA shapes of kernel 7 (with 32-bit words or member and row codes)
+    give the same bits, FP64 and FP32."""
     knobs("ogs.order", 1)
+    knobs("ogs.slab_code_shift", shift)
+    knobs("ogs.slab_row_codes", 1)
     knobs("ogs.slab_load", load)
     ids = O.box_hex_ids(6, 5, 4, 7, 2024)
     h, ref = make(orc, ids)
@@ -166,6 +175,7 @@ def test_slabs_with_16bit_codes(cuda, orc, knobs, box, shift, order, gs_order):
     ids = O.box_hex_ids(nx, ny, nz, p, seed)
     h, ref = make(orc, ids)
     assert h.info.slabCodeShift == shift and h.info.slabCodedEntries > 0
+    assert h.info.slabCodedRows == 0  # row codes are opt-in (ogs.slab_row_codes)
     check_fp64(orc, h, ref, ids.size, 11 + p)
     rs, ci = ref["rsT"], ref["ciT"]
     q = orc.uniform(ids.size, 12).astype(np.float32)
@@ -177,6 +187,42 @@ def test_slabs_with_16bit_codes(cuda, orc, knobs, box, shift, order, gs_order):
         dq = torch.from_numpy(q.copy()).cuda()
         h.GatherScatter(dq, 1, O.Add, O.Sym)
         np.testing.assert_array_equal(host(dq), orc.gather_scatter(rs, ci, rs, ci, q))
+
+
+@pytest.mark.parametrize("box,shift", [((5, 4, 3, 7, 2024), 9), ((7, 3, 2, 1, 0), 3),
+                                       ((4, 3, 5, 3, 77), 12), ((9, 8, 7, 5, 3), 8),
+                                       ((16, 16, 16, 7, 0), 6)])
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("lane", [0, 16])
+def test_slab_row_codes(cuda, orc, knobs, box, shift, order, lane):
+    """The gather's row words as 16-bit codes (ogs.slab_row_codes, with member
+    codes): kernel 7's default Add gather decodes them through each slab's row
+    table, the other shapes and ops read the 32-bit words the plan keeps -- the
+    oracle's bits for every type and op either way (a slab of more than 32 row
+    runs, or one whose codes do not fit 16 bits, keeps its words; order 2 renumbers
+    the walk, so its rows are the plan's permuted row words)."""
+    nx, ny, nz, p, seed = box
+    knobs("ogs.order", order)
+    knobs("ogs.slab_lane", lane)
+    knobs("ogs.slab_code_shift", shift)
+    ids = O.box_hex_ids(nx, ny, nz, p, seed)
+    rng = np.random.default_rng(p)
+    for rc in (1, 0):
+        knobs("ogs.slab_row_codes", rc)
+        h, ref = make(orc, ids)
+        assert (h.info.slabCodedRows > 0) == bool(rc)
+        assert h.info.slabCodedRows <= h.info.NrowsT
+        rs, ci = ref["rsT"], ref["ciT"]
+        for dt, tdt in ((np.float64, torch.float64), (np.float32, torch.float32),
+                        (np.int32, torch.int32), (np.int64, torch.int64)):
+            if dt in (np.float64, np.float32):
+                q = rng.uniform(-1, 1, ids.size).astype(dt)
+            else:
+                q = rng.integers(-9, 10, ids.size).astype(dt)
+            for op in (O.Add, O.Mul, O.Max, O.Min):
+                gq = torch.zeros(rs.size - 1, dtype=tdt, device="cuda")
+                h.Gather(gq, torch.from_numpy(q).cuda(), 1, op, O.Trans)
+                np.testing.assert_array_equal(host(gq), orc.gather(rs, ci, q, 1, op))
 
 
 @pytest.mark.parametrize("k64,k32", [(2, 7), (7, 2), (7, -1)])

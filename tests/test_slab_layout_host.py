@@ -1,10 +1,12 @@
-"""The lane-row slab layout of kernel 7 on the host (no GPU): build_slabs and
-compress_slabs (streamparanumal_gb300/csrc/sp_ogs_order.cpp) are compiled with a
+"""The lane-row slab layout of kernel 7 on the host (no GPU): build_slabs,
+compress_slabs and compress_slab_rows (streamparanumal_gb300/csrc/sp_ogs_order.cpp)
+are compiled with a
 checker (tests/native/slab_layout_check.cpp) that walks every slab the way the
 kernel's index arithmetic does -- full passes of 8 and 16 members per lane, the
 row steps of a slab's rest, any row size, 16-bit codes decoded through the slab's
-table -- checks every index against its array and the results against the
-CSR-order sums bit for bit, for the gather and the in-place gather+scatter."""
+table, row codes through the slab's row table -- checks every index against its
+array and the results against the CSR-order sums bit for bit, for the gather and
+the in-place gather+scatter."""
 import subprocess
 from pathlib import Path
 
@@ -37,8 +39,8 @@ def run(checker, tmp_path, rs, ci, n, order=1, page=9, ball=0, seg=14, shift=0):
                           str(n), str(order), str(page), str(ball), str(seg), str(shift)],
                          capture_output=True, text=True)
     assert res.returncode == 0 and res.stdout.startswith("ok"), res.stdout + res.stderr
-    coded, total = (int(x) for x in res.stdout.split()[2::2])
-    return coded, total
+    coded, total, rows_coded, nrows = (int(x) for x in res.stdout.split()[2::2])
+    return coded, total, rows_coded, nrows
 
 
 BOXES = [((2, 2, 2, 1, 0), 3), ((5, 4, 3, 7, 2024), 9), ((6, 6, 6, 2, 5), 5),
@@ -51,10 +53,11 @@ def test_slab_layout_of_box_meshes(orc, checker, tmp_path, box, shift, order, se
     nx, ny, nz, p, seed = box
     ids = O.box_hex_ids(nx, ny, nz, p, seed)
     csr = orc.ogs_setup(ids.copy(), kind=1, unique=True)
-    coded, total = run(checker, tmp_path, csr["rsT"], csr["ciT"], ids.size, order=order, seg=seg,
-                       shift=shift)
-    # elements of (p+1)^3 <= 2^shift nodes: nearly every slab compresses
+    coded, total, rows_coded, nrows = run(checker, tmp_path, csr["rsT"], csr["ciT"], ids.size,
+                                          order=order, seg=seg, shift=shift)
+    # elements of (p+1)^3 <= 2^shift nodes: nearly every slab compresses, ids and rows
     assert total == 2 * ids.size and coded >= 0.6 * total
+    assert nrows == csr["rsT"].size - 1 and rows_coded >= 0.6 * nrows
 
 
 @pytest.mark.parametrize("seg,shift", [(8, 0), (8, 9), (14, 12), (14, 3)])
