@@ -7,9 +7,13 @@
 // gather+scatter they imply are compared bit for bit with the CSR-order sums.
 //
 // usage: slab_layout_check rs.bin ci.bin N order page_shift ball_shift seg_shift code_shift
+//        [row_perm_seed]   (nonzero: the row words are a seeded permutation of the
+//                           rows, as a renumbered walk folds its permutation in)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <numeric>
 #include <random>
 #include <vector>
 
@@ -154,6 +158,7 @@ int main(int argc, char** argv) {
   const int32_t N = std::atoi(argv[3]);
   const int order = std::atoi(argv[4]), page = std::atoi(argv[5]), ball = std::atoi(argv[6]);
   const int seg = std::atoi(argv[7]), shift = std::atoi(argv[8]);
+  const unsigned row_seed = argc > 9 ? (unsigned)std::atoi(argv[9]) : 0u;
   const int32_t nrows = (int32_t)rs.size() - 1;
   std::vector<int32_t> pairs;
   if (!build_chunks(nrows, rs.data(), ci.data(), N, order, pairs, page, ball)) return 4;
@@ -174,10 +179,15 @@ int main(int argc, char** argv) {
     want_g[r] = acc;
     for (int32_t i = rs[r]; i < rs[r + 1]; ++i) want_gs[ci[i]] = acc;
   }
+  // row words: the rows themselves, or a seeded permutation of them
+  std::vector<int32_t> perm(nrows);
+  std::iota(perm.begin(), perm.end(), 0);
+  if (row_seed) std::shuffle(perm.begin(), perm.end(), std::mt19937(row_seed));
   long coded = 0, total = 0, rows_coded = 0;
   for (int gather = 0; gather < 2; ++gather) {
     Layout L;
-    build_slabs(quads, rs.data(), ci.data(), nullptr, seg, gather == 1, L.desc, L.ids, L.rows);
+    build_slabs(quads, rs.data(), ci.data(), row_seed ? perm.data() : nullptr, seg, gather == 1,
+                L.desc, L.ids, L.rows);
     if (shift > 0) {
       compress_slabs(L.desc, L.ids, shift, L.codes, L.tabs, L.td);
       L.shift = shift;
@@ -201,7 +211,8 @@ int main(int argc, char** argv) {
       walk(L, KB, sink);
       if (gather) {
         for (int32_t r = 0; r < nrows; ++r)
-          CHECK(std::memcmp(&gv[r], &want_g[r], 8) == 0 || (rs[r] == rs[r + 1] && gv[r] == 0.0),
+          CHECK(std::memcmp(&gv[perm[r]], &want_g[r], 8) == 0 ||
+                    (rs[r] == rs[r + 1] && gv[perm[r]] == 0.0),
                 "gather row %d differs (KB %d)", r, KB);
       } else {
         CHECK(std::memcmp(out.data(), want_gs.data(), 8 * out.size()) == 0,

@@ -32,11 +32,12 @@ def checker(tmp_path_factory):
     return out
 
 
-def run(checker, tmp_path, rs, ci, n, order=1, page=9, ball=0, seg=14, shift=0):
+def run(checker, tmp_path, rs, ci, n, order=1, page=9, ball=0, seg=14, shift=0, row_seed=0):
     (tmp_path / "rs.bin").write_bytes(np.ascontiguousarray(rs, dtype=np.int32).tobytes())
     (tmp_path / "ci.bin").write_bytes(np.ascontiguousarray(ci, dtype=np.int32).tobytes())
     res = subprocess.run([str(checker), str(tmp_path / "rs.bin"), str(tmp_path / "ci.bin"),
-                          str(n), str(order), str(page), str(ball), str(seg), str(shift)],
+                          str(n), str(order), str(page), str(ball), str(seg), str(shift),
+                          str(row_seed)],
                          capture_output=True, text=True)
     assert res.returncode == 0 and res.stdout.startswith("ok"), res.stdout + res.stderr
     coded, total, rows_coded, nrows = (int(x) for x in res.stdout.split()[2::2])
@@ -68,3 +69,20 @@ def test_slab_layout_any_row_size_and_empty_rows(orc, checker, tmp_path, seg, sh
     rs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
     ci = rng.permutation(n).astype(np.int32)
     run(checker, tmp_path, rs, ci, n, order=0, seg=seg, shift=shift)
+
+
+@pytest.mark.parametrize("box,shift", [((5, 4, 3, 7, 2024), 9), ((6, 6, 6, 2, 5), 5)])
+def test_slab_row_words_beyond_the_row_table(orc, checker, tmp_path, box, shift):
+    """Row words that a seeded permutation scatters over the whole row range: a slab
+    whose rows fall into more than 32 runs (or whose codes do not fit 16 bits)
+    keeps its 32-bit row words, the others decode through their row table, and the
+    gather still lands every row's sum on its permuted row word."""
+    nx, ny, nz, p, seed = box
+    ids = O.box_hex_ids(nx, ny, nz, p, seed)
+    csr = orc.ogs_setup(ids.copy(), kind=1, unique=True)
+    rs, ci = csr["rsT"], csr["ciT"]
+    _, _, rows_sorted, nrows = run(checker, tmp_path, rs, ci, ids.size, shift=shift)
+    _, _, rows_perm, nrows_p = run(checker, tmp_path, rs, ci, ids.size, shift=shift, row_seed=17)
+    assert nrows == nrows_p == rs.size - 1
+    # first-appearance rows fall into few runs; permuted ones mostly do not
+    assert rows_sorted >= 0.6 * nrows and rows_perm < 0.5 * nrows
