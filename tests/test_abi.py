@@ -149,3 +149,30 @@ def test_tuning_knobs_ranges_and_defaults(lib, key):
 
 def test_unknown_knob_is_rejected(lib):
     assert capi.status("sp_tune_set", b"ogs.no_such_knob", 0) == capi.SP_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("cname,pyname", [("sp_ogs_info", "capi.OgsInfo"),
+                                          ("sp_ogs_mr_info", "capi.MrInfo"),
+                                          ("sp_ogs_mr_sched", "capi.MrSched"),
+                                          ("sp_comm", "comm.SpComm")])
+def test_ctypes_structs_match_the_header(tmp_path, cname, pyname):
+    """The ctypes mirrors of the ABI's structs have the header's size and field
+    offsets (a C program compiled against include/sp_capi.h prints them)."""
+    from pathlib import Path
+    from streamparanumal_gb300 import comm
+    mod, cls = pyname.split(".")
+    st = getattr({"capi": capi, "comm": comm}[mod], cls)
+    fields = [f[0] for f in st._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"sp_capi.h\"\n"
+                   "int main(void) {\n"
+                   f"  printf(\"%zu\\n\", sizeof({cname}));\n" +
+                   "".join(f"  printf(\"%zu\\n\", offsetof({cname}, {f}));\n" for f in fields) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    include = Path(capi.__file__).resolve().parent.parent / "include"
+    subprocess.run(["gcc", "-std=c11", f"-I{include}", str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(st)
+    assert got[1:] == [getattr(st, f).offset for f in fields]
